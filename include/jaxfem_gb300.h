@@ -1,0 +1,210 @@
+/*
+ * jaxfem_gb300.h -- C ABI of the GB300 (sm_103a) implementation of jax-fem's
+ * hot path: per-cell weak form at quadrature points, scatter-add assembly of
+ * the residual and the CSR Jacobian, the Krylov solve and the implicit adjoint.
+ *
+ * The reference (deepmodeling/jax-fem) is pure Python on JAX/PETSc and has no
+ * native FFI of its own; each entry point below replaces the reference
+ * function(s) cited beside it (paths relative to the jax-fem repository).
+ *
+ * Conventions (all entry points):
+ *   - return an int status: FEM_OK (0) or an FEM_ERR_* code; the message is
+ *     available from fem_last_error() on the calling thread;
+ *   - take raw DEVICE pointers, sizes and an opaque CUDA stream (`void*`,
+ *     a cudaStream_t; NULL = legacy default stream); work is enqueued on that
+ *     stream and nothing is synchronised unless stated (calls that return a
+ *     host-side count or status synchronise the stream);
+ *   - never allocate device memory: every workspace is caller-owned, sized by
+ *     the matching *_workspace() query;
+ *   - degrees of freedom are ordered dof = node*vec + component
+ *     (jax_fem/problem.py:86-92), matrices are CSR with rows sorted by column.
+ *   - not re-entrant on the same workspace; one stream per problem.
+ */
+#ifndef JAXFEM_GB300_H
+#define JAXFEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+  FEM_OK = 0,
+  FEM_ERR_ARG = 1,         /* invalid argument (null pointer, bad size, bad enum) */
+  FEM_ERR_CUDA = 2,        /* a CUDA runtime call or kernel launch failed        */
+  FEM_ERR_UNSUPPORTED = 3, /* element / material / precision combination absent  */
+  FEM_ERR_CAPACITY = 4,    /* workspace too small or a row exceeds 255 blocks    */
+  FEM_ERR_DEVICE = 5       /* a kernel reported invalid data (e.g. bad node id)  */
+};
+
+/* ---- enumerations -------------------------------------------------------- */
+enum { FEM_HEX8 = 1, FEM_TET10 = 2, FEM_TET4 = 3 };          /* jax_fem/basis.py:19-114 */
+enum { FEM_F32 = 0, FEM_F64 = 1 };
+enum {                                                       /* built-in tensor maps     */
+  FEM_MAT_LAPLACE = 1,        /* consts: [k]                      test_linear_poisson.py:15-17 */
+  FEM_MAT_LINEAR_ELASTIC = 2, /* consts: [E, nu]                  test_linear_elasticity_cube.py:15-26 */
+  FEM_MAT_SIMP = 3,           /* consts: [Emax, Emin, nu, penal]; qp param theta */
+  FEM_MAT_GENERAL_LINEAR = 4, /* consts: C ((vec*3)^2, row-major) sigma_I = C_IJ grad_J */
+  FEM_MAT_NEO_HOOKEAN = 5,    /* consts: [E, nu, clampJ]; optional qp param rho (E*rho)
+                                 test_hyper_elasticity.py:15-34, hyperelastic3d_common.py:45-70 */
+  FEM_MAT_J2 = 6              /* consts: [E, nu, sig0]; history sigma_old|eps_old (18/qp);
+                                 optional qp param s scaling E      test_plasticity.py:32-78 */
+};
+enum { FEM_OUT_RESIDUAL = 1, FEM_OUT_MATRIX = 2, FEM_OUT_APPLY = 4 };
+enum {
+  FEM_BC_NONE = 0,
+  FEM_BC_ROWS = 1,      /* skip Dirichlet rows (PETSc zeroRows semantics, solver.py:527-528) */
+  FEM_BC_SYMMETRIC = 2  /* skip Dirichlet rows and columns (symmetric elimination for CG) */
+};
+enum { FEM_PC_NONE = 0, FEM_PC_JACOBI = 1, FEM_PC_BJACOBI = 2 };
+enum { FEM_SOLVE_CONVERGED = 0, FEM_SOLVE_MAXITER = 1, FEM_SOLVE_BREAKDOWN = 2, FEM_SOLVE_NAN = 3 };
+
+/* ---- plain descriptor structs (pointers are device pointers) ------------- */
+typedef struct fem_mesh_t {
+  int32_t elem_type;        /* FEM_HEX8 / FEM_TET10 / FEM_TET4                   */
+  int32_t vec;              /* components per node: 1 or 3                        */
+  int64_t n_nodes;
+  int64_t n_cells;
+  const double* coords;     /* (n_nodes, 3)                                       */
+  const int32_t* conn;      /* (n_cells, nodes_per_cell), meshio node order       */
+} fem_mesh_t;
+
+typedef struct fem_pattern_t {
+  int64_t nnzb;             /* number of node-pair blocks                         */
+  const int64_t* block_ptr; /* (n_nodes+1)                                        */
+  const int32_t* block_cols;/* (nnzb), sorted within each node row               */
+  const int64_t* indptr;    /* scalar CSR row pointers (n_nodes*vec+1)            */
+  const int64_t* diag;      /* (n_nodes*vec) offset of each row's diagonal entry  */
+  const uint8_t* slots;     /* (n_cells, npc, npc): position of conn[b] in row conn[a] */
+} fem_pattern_t;
+
+typedef struct fem_material_t {
+  int32_t kind;             /* FEM_MAT_*                                          */
+  int32_t n_consts;         /* <= 96                                              */
+  const double* consts;     /* HOST pointer, copied at call time                  */
+  int32_t n_qp_params;      /* per quadrature point parameters (0 or 1)           */
+  const double* qp_params;  /* (n_cells, nq, n_qp_params) or NULL                 */
+  const double* history;    /* J2: (n_cells, nq, 18) = sigma_old(9) | eps_old(9)  */
+} fem_material_t;
+
+/* ---- library ------------------------------------------------------------- */
+const char* fem_last_error(void);
+int fem_version(void);
+/* Element sizes: nodes per cell, volume quad points, faces, face quad points. */
+int fem_element_info(int32_t elem_type, int32_t* nodes_per_cell, int32_t* n_quads,
+                     int32_t* n_faces, int32_t* n_face_quads);
+
+/* Reference-element tables in double precision, written to HOST arrays (any may be NULL):
+ * N (nq,nn), dN (nq,nn,3), w (nq), face_N (nf,nfq,nn), face_dN (nf,nfq,nn,3), face_w (nf,nfq),
+ * face_normals (nf,3), face_inds (nf,nfv).  Replaces jax_fem/basis.py:141-250 (basix tabulation). */
+int fem_element_tables(int32_t elem_type, double* N, double* dN, double* w, double* face_N, double* face_dN,
+                       double* face_w, double* face_normals, int32_t* face_inds);
+
+/* ---- sparsity pattern ----------------------------------------------------
+ * Replaces the COO index build jax_fem/problem.py:86-107 and PETSc's COO
+ * preallocation jax_fem/solver.py:474-478: the pattern is the sorted union of
+ * every cell's dof pairs, kept as node-pair blocks (each block is vec x vec
+ * and fully populated) plus the equivalent scalar CSR row pointers.  */
+int fem_pattern_workspace(int64_t n_cells, int32_t nodes_per_cell, int64_t n_nodes, size_t* bytes);
+/* Builds node->cell incidence in ws, writes block_ptr and the total block count (host). Syncs. */
+int fem_pattern_count(int32_t elem_type, const int32_t* conn, int64_t n_cells, int64_t n_nodes,
+                      void* ws, size_t ws_bytes, int64_t* block_ptr, int64_t* nnzb_out, void* stream);
+/* Fills block_cols (nnzb); ws must hold what fem_pattern_count left there. */
+int fem_pattern_fill(int32_t elem_type, const int32_t* conn, int64_t n_cells, int64_t n_nodes,
+                     void* ws, size_t ws_bytes, const int64_t* block_ptr, int32_t* block_cols, void* stream);
+/* Per-cell block slots: slots[c][a][b] = position of conn[c][b] in row conn[c][a]. */
+int fem_pattern_slots(int32_t elem_type, const int32_t* conn, int64_t n_cells,
+                      const int64_t* block_ptr, const int32_t* block_cols, uint8_t* slots, void* stream);
+/* Scalar CSR view: indptr (n_nodes*vec+1), diag (n_nodes*vec), indices (nnzb*vec*vec, may be NULL). */
+int fem_pattern_scalar(int64_t n_nodes, int32_t vec, const int64_t* block_ptr, const int32_t* block_cols,
+                       int64_t* indptr, int64_t* diag, int32_t* indices, void* stream);
+
+/* ---- geometry and loads ---------------------------------------------------
+ * Replaces jax_fem/fe.py:112-218 (shape grads, JxW, physical quad points,
+ * face Nanson scale) and the u-independent parts of the mass / surface
+ * kernels jax_fem/problem.py:216-259. */
+int fem_quad_points(const fem_mesh_t* mesh, double* x_out /* (n_cells,nq,3) */,
+                    double* jxw_out /* (n_cells,nq) or NULL */, void* stream);
+int fem_face_quad_points(const fem_mesh_t* mesh, const int32_t* face_cells, const int32_t* face_ids,
+                         int64_t n_faces, double* x_out /* (n_faces,nfq,3) */,
+                         double* nanson_out /* (n_faces,nfq) or NULL */, void* stream);
+/* out[dof] += sum_q f_qp[c,q,:] N_a(q) JxW  (mass_map evaluated at quad points) */
+int fem_body_load(const fem_mesh_t* mesh, const double* f_qp, double* out, void* stream);
+/* out[dof] += sum_q t_qp[f,q,:] N_a(q) nanson  (surface_map at face quad points) */
+int fem_surface_load(const fem_mesh_t* mesh, const int32_t* face_cells, const int32_t* face_ids,
+                     int64_t n_faces, const double* t_qp, double* out, void* stream);
+
+/* ---- per-cell weak form and assembly --------------------------------------
+ * Replaces the cell kernels and their jacfwd tangents jax_fem/problem.py:189-303,
+ * the batched evaluation split_and_compute_cell :359-396, the residual scatter
+ * compute_residual_vars_helper :426-437, compute_newton_vars :447-460 and the
+ * PETSc setValuesCOO/assemble jax_fem/solver.py:522-526.
+ * outputs: FEM_OUT_RESIDUAL  residual += R_int(u)           (FP64 always)
+ *          FEM_OUT_MATRIX    vals += K(u) in `precision`    (consistent hand-derived tangent)
+ *          FEM_OUT_APPLY     apply_out += K(u) w            (FP64 always)
+ * Outputs are accumulated (the caller zeroes them).  bc_mode controls which
+ * matrix entries are skipped (FEM_BC_*); bc_mask is one byte per dof.  With a
+ * bc_mask, FEM_OUT_RESIDUAL / FEM_OUT_APPLY skip Dirichlet rows too. */
+int fem_assemble(const fem_mesh_t* mesh, const fem_material_t* mat, const fem_pattern_t* pat,
+                 int32_t outputs, int32_t precision, const double* u, const double* w,
+                 const uint8_t* bc_mask, int32_t bc_mode, double* residual, void* vals,
+                 double* apply_out, void* stream);
+
+/* Parameter VJP (replaces the jax.vjp of the BC-applied residual w.r.t. params in
+ * implicit_vjp, jax_fem/solver.py:1386-1416):
+ *   grad_qp[c,q,k] = - sum_a lam_a . dR_a/dp_{c,q,k}   (lam masked to 0 on Dirichlet dofs). */
+int fem_param_vjp(const fem_mesh_t* mesh, const fem_material_t* mat, const double* u,
+                  const double* lam, const uint8_t* bc_mask, double* grad_qp, void* stream);
+
+/* J2 history update (tests/benchmarks/plasticity/test_plasticity.py:73-78):
+ * history_out[c,q] = (return_map(grad u, history), strain(grad u)). */
+int fem_j2_update(const fem_mesh_t* mesh, const fem_material_t* mat, const double* u,
+                  double* history_out, void* stream);
+
+/* ---- Dirichlet rows -------------------------------------------------------
+ * fem_zero_rows: PETSc zeroRows with KEEP_NONZERO_PATTERN (solver.py:477,527-528):
+ *   every entry of each listed row := 0, then the diagonal := diag_value.
+ * fem_apply_bc_vec: apply_bc_vec (solver.py:290-304): res[r] = dofs[r] - scale*vals[i]. */
+int fem_zero_rows(const fem_pattern_t* pat, int32_t vec, int32_t precision, void* vals,
+                  const int32_t* rows, int64_t n_rows, double diag_value, void* stream);
+int fem_apply_bc_vec(double* res, const double* dofs, const int32_t* rows, const double* values,
+                     int64_t n_rows, double scale, void* stream);
+
+/* ---- sparse linear algebra ------------------------------------------------
+ * Replaces jax.scipy.sparse.linalg.bicgstab on the BCOO matrix (solver.py:63-92)
+ * and PETSc KSPCG/KSPBCGS with PCJACOBI / PCBJACOBI (solver.py:109-134). */
+int fem_spmv(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
+             const void* vals, const void* x, void* y, void* stream);
+/* Jacobi: pc = 1/diag (n_dofs values); block Jacobi: inverse node blocks (n_nodes*vec*vec). */
+int fem_precond_setup(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
+                      const void* vals, int32_t pc_kind, void* pc, void* stream);
+int fem_krylov_workspace(int64_t n_dofs, int32_t precision, size_t* bytes);
+/* Preconditioned CG on an SPD matrix.  Stops when ||r||_2 <= max(rtol*||b||_2, atol)
+ * (checked every iteration on the device; dots and norms in FP64).  Syncs. */
+int fem_pcg(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
+            const void* vals, int32_t pc_kind, const void* pc, const void* b, void* x,
+            double rtol, double atol, int64_t maxiter, void* ws, size_t ws_bytes,
+            int64_t* iterations, double* res_norm, int32_t* status, void* stream);
+/* BiCGStab with jax.scipy.sparse.linalg.bicgstab's iteration and stopping rule
+ * ||r||^2 <= max(tol^2 ||b||^2, atol^2) (solver.py:78-84).  Syncs. */
+int fem_bicgstab(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
+                 const void* vals, int32_t pc_kind, const void* pc, const void* b, void* x,
+                 double tol, double atol, int64_t maxiter, void* ws, size_t ws_bytes,
+                 int64_t* iterations, double* res_norm, int32_t* status, void* stream);
+
+/* ---- vector helpers for refinement / Newton ------------------------------ */
+/* dst32[i] = mask[i] ? 0 : (float)src64[i]  (mask may be NULL) */
+int fem_cast_f64_f32(const double* src, float* dst, int64_t n, const uint8_t* mask, void* stream);
+/* y64[i] += alpha * (double)x32[i] */
+int fem_axpy_f32_f64(double alpha, const float* x, double* y, int64_t n, void* stream);
+/* Deterministic FP64 dot product written to *out (device); ws >= fem_krylov_workspace bytes. */
+int fem_dot(int32_t precision, const void* x, const void* y, int64_t n, double* out,
+            void* ws, size_t ws_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JAXFEM_GB300_H */

@@ -1,0 +1,358 @@
+// Per-cell weak-form kernel: residual, consistent tangent (CSR values) and
+// tangent action, evaluated at quadrature points and scattered into global
+// arrays.  Restates the per-cell work of jax_fem/problem.py:189-303
+// (laplace kernel + jacfwd tangent) and the scatter :426-437 / PETSc
+// setValuesCOO (jax_fem/solver.py:525) as one fused pass.
+//
+// One CTA processes CPB cells per tile (grid-stride over tiles):
+//   A  load connectivity, cell-local coordinates (x - x_node0, in FP64, then T),
+//      nodal u (and w) into shared memory                 (thread per cell node)
+//   B  geometry at each quadrature point: J, det, J^-1, physical shape grads,
+//      JxW; material stress/tangent pre-scaled by JxW    (thread per cell qp)
+//   C  element matrix rows K[(a,i),:] and atomic scatter into the CSR value
+//      slots given by the per-cell slot table             (thread per cell row)
+//   D  element residual / tangent action rows, pre-reduced across the warp
+//      (lanes hitting the same dof are summed first), then FP64 atomics.
+#pragma once
+
+#include "fem_common.cuh"
+#include "fem_elements.cuh"
+#include "fem_materials.cuh"
+
+namespace fem {
+
+struct AsmParams {
+  VolTables tab;
+  MatConsts mc;
+  const double* coords;
+  const int32_t* conn;
+  int64_t n_cells;
+  const double* u;
+  const double* w;
+  const double* qp_params;
+  int n_qp;
+  const double* hist;
+  const int64_t* indptr;
+  const uint8_t* slots;
+  const uint8_t* bc;
+  int bc_mode;
+  int outputs;            // FEM_OUT_* bits handled by this launch
+  double* res;
+  void* vals;
+  double* apply_out;
+  double* vjp_out;        // fem_param_vjp
+  double* hist_out;       // fem_j2_update
+};
+
+enum { KMODE_ASSEMBLE = 0, KMODE_VJP = 1, KMODE_HIST = 2 };
+
+template <int NN, int VEC>
+struct Cpb {
+  static constexpr int value = (192 / (NN * VEC)) > 0 ? (192 / (NN * VEC)) : 1;
+};
+
+template <int NN, int NQ, int VEC, int MAT, typename T>
+struct AsmLayout {
+  static constexpr int CPB = Cpb<NN, VEC>::value;
+  static constexpr int THREADS = ((CPB * NN * VEC + 31) / 32) * 32;   // full warps
+  static constexpr int NTAN = MatTraits<MAT, VEC>::NTAN;
+  static constexpr int NS = VEC * 3;
+  // offsets in elements of T
+  static constexpr int oN = 0;
+  static constexpr int odN = oN + NQ * NN;
+  static constexpr int oX = odN + NQ * NN * 3;
+  static constexpr int oU = oX + CPB * NN * 3;
+  static constexpr int oW = oU + CPB * NN * VEC;
+  static constexpr int oG = oW + CPB * NN * VEC;
+  static constexpr int oS = oG + CPB * NQ * NN * 3;
+  static constexpr int oTan = oS + CPB * NQ * NS;
+  static constexpr int nT = oTan + CPB * NQ * NTAN;
+  static constexpr size_t bytes = sizeof(T) * (size_t)nT + sizeof(int) * CPB * NN + sizeof(double) * THREADS + 16;
+};
+
+template <int NN, int NQ, int VEC, int MAT, typename T, int KMODE>
+__global__ void __launch_bounds__(AsmLayout<NN, NQ, VEC, MAT, T>::THREADS)
+cell_kernel(const AsmParams P) {
+  using L = AsmLayout<NN, NQ, VEC, MAT, T>;
+  using Mat = Material<MAT, VEC, T>;
+  constexpr int CPB = L::CPB, NS = L::NS, NTAN = L::NTAN;
+  constexpr int TAN = MatTraits<MAT, VEC>::TAN;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  T* sN = sm + L::oN;
+  T* sdN = sm + L::odN;
+  T* sX = sm + L::oX;
+  T* sU = sm + L::oU;
+  T* sW = sm + L::oW;
+  T* sG = sm + L::oG;
+  T* sS = sm + L::oS;
+  T* sTan = sm + L::oTan;
+  int* sConn = reinterpret_cast<int*>(sm + L::nT);
+  double* sRed = reinterpret_cast<double*>(
+      (reinterpret_cast<uintptr_t>(sConn + CPB * NN) + 15) & ~uintptr_t(15));
+
+  const int tid = threadIdx.x;
+  for (int k = tid; k < NQ * NN; k += blockDim.x) {
+    const int q = k / NN, n = k % NN;
+    sN[k] = T(P.tab.N[q][n]);
+    for (int d = 0; d < 3; ++d) sdN[k * 3 + d] = T(P.tab.dN[q][n][d]);
+  }
+
+  const bool want_res = (KMODE == KMODE_ASSEMBLE) && (P.outputs & FEM_OUT_RESIDUAL);
+  const bool want_mat = (KMODE == KMODE_ASSEMBLE) && (P.outputs & FEM_OUT_MATRIX);
+  const bool want_app = (KMODE == KMODE_ASSEMBLE) && (P.outputs & FEM_OUT_APPLY);
+  const bool need_w = want_app || KMODE == KMODE_VJP;
+
+  const int64_t n_tiles = (P.n_cells + CPB - 1) / CPB;
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    __syncthreads();
+    // ---- A: gather -------------------------------------------------------
+    for (int k = tid; k < CPB * NN; k += blockDim.x) {
+      const int c = k / NN, n = k % NN;
+      const int64_t e = tile * CPB + c;
+      int node = -1;
+      if (e < P.n_cells) node = P.conn[e * NN + n];
+      sConn[k] = node;
+      if (node >= 0) {
+        const int n0 = P.conn[e * NN];
+        for (int d = 0; d < 3; ++d) sX[k * 3 + d] = T(P.coords[(int64_t)node * 3 + d] - P.coords[(int64_t)n0 * 3 + d]);
+        for (int v = 0; v < VEC; ++v) {
+          const int64_t dof = (int64_t)node * VEC + v;
+          sU[k * VEC + v] = P.u ? T(P.u[dof]) : T(0);
+          if (need_w) {
+            T wv = T(P.w[dof]);
+            if (KMODE == KMODE_VJP && P.bc && P.bc[dof]) wv = T(0);
+            sW[k * VEC + v] = wv;
+          }
+        }
+      } else {
+        for (int d = 0; d < 3; ++d) sX[k * 3 + d] = T(0);
+        for (int v = 0; v < VEC; ++v) { sU[k * VEC + v] = T(0); if (need_w) sW[k * VEC + v] = T(0); }
+      }
+    }
+    __syncthreads();
+    // ---- B: geometry + material at quadrature points ----------------------
+    for (int k = tid; k < CPB * NQ; k += blockDim.x) {
+      const int c = k / NQ, q = k % NQ;
+      const int64_t e = tile * CPB + c;
+      if (e >= P.n_cells) continue;
+      const T* X = sX + c * NN * 3;
+      T J[3][3] = {};
+      for (int n = 0; n < NN; ++n)
+        for (int d = 0; d < 3; ++d) {
+          const T x = X[n * 3 + d];
+          for (int r = 0; r < 3; ++r) J[d][r] += x * sdN[(q * NN + n) * 3 + r];
+        }
+      const T det = det3<T>(J);
+      T Ji[3][3];
+      inv3<T>(J, det, Ji);
+      const T jxw = det * T(P.tab.w[q]);
+      T* G = sG + (c * NQ + q) * NN * 3;
+      T gu[NS];
+      T gw[NS];
+      for (int s = 0; s < NS; ++s) { gu[s] = T(0); gw[s] = T(0); }
+      for (int n = 0; n < NN; ++n) {
+        const T* dn = sdN + (q * NN + n) * 3;
+        T g[3];
+        for (int d = 0; d < 3; ++d) g[d] = dn[0] * Ji[0][d] + dn[1] * Ji[1][d] + dn[2] * Ji[2][d];
+        for (int d = 0; d < 3; ++d) G[n * 3 + d] = g[d];
+        for (int v = 0; v < VEC; ++v) {
+          const T un = sU[(c * NN + n) * VEC + v];
+          for (int d = 0; d < 3; ++d) gu[v * 3 + d] += un * g[d];
+          if (need_w) {
+            const T wn = sW[(c * NN + n) * VEC + v];
+            for (int d = 0; d < 3; ++d) gw[v * 3 + d] += wn * g[d];
+          }
+        }
+      }
+      const double* qp = P.qp_params ? P.qp_params + (e * NQ + q) * P.n_qp : nullptr;
+      const double* hs = P.hist ? P.hist + (e * NQ + q) * 18 : nullptr;
+      if constexpr (KMODE == KMODE_VJP) {
+        T dS[NS];
+        Mat::dparam(gu, P.mc, qp, hs, dS);
+        T acc = T(0);
+        for (int s = 0; s < NS; ++s) acc += dS[s] * gw[s];
+        P.vjp_out[(e * NQ + q) * P.n_qp] = -double(acc) * double(jxw);
+        continue;
+      }
+      if constexpr (KMODE == KMODE_HIST) {
+        if constexpr (VEC == 3) {
+          T S[NS];
+          Mat::eval(gu, P.mc, qp, hs, S, nullptr, false);
+          double* ho = P.hist_out + (e * NQ + q) * 18;
+          for (int s = 0; s < 9; ++s) ho[s] = double(S[s]);
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) ho[9 + i * 3 + j] = 0.5 * (double(gu[i * 3 + j]) + double(gu[j * 3 + i]));
+        }
+        continue;
+      }
+      T S[NS];
+      T* tq = sTan + (c * NQ + q) * NTAN;   // tangent is evaluated straight into shared memory
+      const bool need_tan = want_mat || want_app;
+      Mat::eval(gu, P.mc, qp, hs, S, tq, need_tan);
+      T* Sq = sS + (c * NQ + q) * NS;
+      if (want_app) {
+        // dS = A : grad w  (tangent action), stored in place of the stress
+        if constexpr (TAN == TAN_SCALAR) {
+          for (int s = 0; s < NS; ++s) Sq[s] = tq[0] * gw[s] * jxw;
+        } else if constexpr (TAN == TAN_ISO) {
+          T dS[NS];
+          iso_stress(gw, tq[0], tq[1], dS);
+          for (int s = 0; s < NS; ++s) Sq[s] = dS[s] * jxw;
+        } else {
+          for (int I = 0; I < NS; ++I) {
+            T acc = T(0);
+            for (int Jx = 0; Jx < NS; ++Jx) acc += tq[I * NS + Jx] * gw[Jx];
+            Sq[I] = acc * jxw;
+          }
+        }
+      } else {
+        for (int s = 0; s < NS; ++s) Sq[s] = S[s] * jxw;
+      }
+      if (want_mat)
+        for (int s = 0; s < NTAN; ++s) tq[s] *= jxw;
+    }
+    if constexpr (KMODE != KMODE_ASSEMBLE) continue;
+    __syncthreads();
+    // ---- C / D: element rows ---------------------------------------------
+    const int c = tid / (NN * VEC);
+    const int r = tid % (NN * VEC);
+    const int a = r / VEC, i = r % VEC;
+    const int64_t e = tile * CPB + c;
+    const bool active = (c < CPB) && (e < P.n_cells);
+    const int na = active ? sConn[c * NN + a] : 0;
+    const int64_t row = (int64_t)na * VEC + i;
+    const bool row_bc = active && P.bc && P.bc[row];
+
+    if (want_mat && active && !(row_bc && P.bc_mode != FEM_BC_NONE)) {
+      T acc[NN][VEC];
+      for (int b = 0; b < NN; ++b)
+        for (int k = 0; k < VEC; ++k) acc[b][k] = T(0);
+      for (int q = 0; q < NQ; ++q) {
+        const T* G = sG + (c * NQ + q) * NN * 3;
+        const T ga0 = G[a * 3 + 0], ga1 = G[a * 3 + 1], ga2 = G[a * 3 + 2];
+        const T* tq = sTan + (c * NQ + q) * NTAN;
+        if constexpr (TAN == TAN_SCALAR) {
+          const T t0 = tq[0];
+          for (int b = 0; b < NN; ++b)
+            acc[b][0] += t0 * (ga0 * G[b * 3] + ga1 * G[b * 3 + 1] + ga2 * G[b * 3 + 2]);
+        } else if constexpr (TAN == TAN_ISO) {
+          const T lam = tq[0], mu = tq[1];
+          const T gai = G[a * 3 + i];
+          const T lgi = lam * gai;
+          for (int b = 0; b < NN; ++b) {
+            const T gb0 = G[b * 3], gb1 = G[b * 3 + 1], gb2 = G[b * 3 + 2];
+            const T gbi = G[b * 3 + i];
+            const T mdot = mu * (ga0 * gb0 + ga1 * gb1 + ga2 * gb2);
+            const T mgbi = mu * gbi;
+            acc[b][0] += lgi * gb0 + mgbi * ga0 + (i == 0 ? mdot : T(0));
+            if constexpr (VEC == 3) {
+              acc[b][1] += lgi * gb1 + mgbi * ga1 + (i == 1 ? mdot : T(0));
+              acc[b][2] += lgi * gb2 + mgbi * ga2 + (i == 2 ? mdot : T(0));
+            }
+          }
+        } else {
+          // T_kl = sum_j ga_j A[(i,j),(k,l)]
+          T Tk[VEC][3];
+          for (int k = 0; k < VEC; ++k)
+            for (int l = 0; l < 3; ++l)
+              Tk[k][l] = ga0 * tq[(i * 3 + 0) * NS + k * 3 + l] + ga1 * tq[(i * 3 + 1) * NS + k * 3 + l] +
+                         ga2 * tq[(i * 3 + 2) * NS + k * 3 + l];
+          for (int b = 0; b < NN; ++b) {
+            const T gb0 = G[b * 3], gb1 = G[b * 3 + 1], gb2 = G[b * 3 + 2];
+            for (int k = 0; k < VEC; ++k) acc[b][k] += Tk[k][0] * gb0 + Tk[k][1] * gb1 + Tk[k][2] * gb2;
+          }
+        }
+      }
+      T* vals = reinterpret_cast<T*>(P.vals);
+      const int64_t rs = P.indptr[row];
+      const uint8_t* sl = P.slots + (e * NN + a) * NN;
+      for (int b = 0; b < NN; ++b) {
+        const int nb = sConn[c * NN + b];
+        T* dst = vals + rs + (int64_t)VEC * sl[b];
+        for (int k = 0; k < VEC; ++k) {
+          if (P.bc_mode == FEM_BC_SYMMETRIC && P.bc[(int64_t)nb * VEC + k]) continue;
+          atomicAdd(dst + k, acc[b][k]);
+        }
+      }
+    }
+
+    if (want_res || want_app) {
+      double rv = 0.0;
+      if (active) {
+        T s = T(0);
+        for (int q = 0; q < NQ; ++q) {
+          const T* G = sG + (c * NQ + q) * NN * 3;
+          const T* Sq = sS + (c * NQ + q) * NS;
+          s += Sq[i * 3 + 0] * G[a * 3 + 0] + Sq[i * 3 + 1] * G[a * 3 + 1] + Sq[i * 3 + 2] * G[a * 3 + 2];
+        }
+        rv = double(s);
+      }
+      // warp-segmented pre-reduction: lanes with the same destination dof are
+      // summed (in lane order) before one FP64 atomic per distinct dof
+      const bool emit = active && !row_bc;
+      const long long key = emit ? (long long)row : -1 - (long long)(tid & 31);
+      const unsigned grp = __match_any_sync(0xffffffffu, key);
+      sRed[tid] = rv;
+      __syncwarp();
+      const int lane = tid & 31;
+      if (emit && lane == __ffs(grp) - 1) {
+        double sum = 0.0;
+        for (unsigned m = grp; m; m &= m - 1) sum += sRed[(tid & ~31) + __ffs(m) - 1];
+        atomicAdd(want_res ? (P.res + row) : (P.apply_out + row), sum);
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Host-side launcher for one (element, vec, material, precision, mode).
+template <int NN, int NQ, int VEC, int MAT, typename T, int KMODE>
+int launch_cell_kernel(const AsmParams& P, cudaStream_t stream) {
+  using L = AsmLayout<NN, NQ, VEC, MAT, T>;
+  auto kern = cell_kernel<NN, NQ, VEC, MAT, T, KMODE>;
+  const size_t smem = L::bytes;
+  if (smem > 48 * 1024) FEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t tiles = (P.n_cells + L::CPB - 1) / L::CPB;
+  int blocks_per_sm = 1;
+  FEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, L::THREADS, smem));
+  if (blocks_per_sm < 1) blocks_per_sm = 1;
+  int64_t grid = (int64_t)sm_count() * blocks_per_sm;
+  if (grid > tiles) grid = tiles;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, L::THREADS, smem, stream>>>(P);
+  return check_launch("cell_kernel");
+}
+
+template <int NN, int NQ, int VEC, int MAT>
+int dispatch_precision(const AsmParams& P, int precision, int kmode, cudaStream_t s) {
+  if (kmode == KMODE_VJP) return launch_cell_kernel<NN, NQ, VEC, MAT, double, KMODE_VJP>(P, s);
+  if (kmode == KMODE_HIST) return launch_cell_kernel<NN, NQ, VEC, MAT, double, KMODE_HIST>(P, s);
+  if (precision == FEM_F32) return launch_cell_kernel<NN, NQ, VEC, MAT, float, KMODE_ASSEMBLE>(P, s);
+  return launch_cell_kernel<NN, NQ, VEC, MAT, double, KMODE_ASSEMBLE>(P, s);
+}
+
+template <int NN, int NQ>
+int dispatch_material(const AsmParams& P, int vec, int mat, int precision, int kmode, cudaStream_t s) {
+  if (vec == 1) {
+    if (mat == FEM_MAT_LAPLACE) return dispatch_precision<NN, NQ, 1, FEM_MAT_LAPLACE>(P, precision, kmode, s);
+    if (mat == FEM_MAT_GENERAL_LINEAR) return dispatch_precision<NN, NQ, 1, FEM_MAT_GENERAL_LINEAR>(P, precision, kmode, s);
+  } else if (vec == 3) {
+    switch (mat) {
+      case FEM_MAT_LINEAR_ELASTIC: return dispatch_precision<NN, NQ, 3, FEM_MAT_LINEAR_ELASTIC>(P, precision, kmode, s);
+      case FEM_MAT_SIMP: return dispatch_precision<NN, NQ, 3, FEM_MAT_SIMP>(P, precision, kmode, s);
+      case FEM_MAT_GENERAL_LINEAR: return dispatch_precision<NN, NQ, 3, FEM_MAT_GENERAL_LINEAR>(P, precision, kmode, s);
+      case FEM_MAT_NEO_HOOKEAN: return dispatch_precision<NN, NQ, 3, FEM_MAT_NEO_HOOKEAN>(P, precision, kmode, s);
+      case FEM_MAT_J2: return dispatch_precision<NN, NQ, 3, FEM_MAT_J2>(P, precision, kmode, s);
+      default: break;
+    }
+  }
+  return fail(FEM_ERR_UNSUPPORTED, "material/vec combination not supported");
+}
+
+// per-element-type entry points (one translation unit each, compiled in parallel)
+int assemble_hex8(const AsmParams& P, int vec, int mat, int precision, int kmode, cudaStream_t s);
+int assemble_tet10(const AsmParams& P, int vec, int mat, int precision, int kmode, cudaStream_t s);
+int assemble_tet4(const AsmParams& P, int vec, int mat, int precision, int kmode, cudaStream_t s);
+
+}  // namespace fem

@@ -1,0 +1,346 @@
+"""Device-side state of a Problem and thin wrappers over the C ABI.
+
+One Engine per Problem owns every device buffer of the hot path: mesh,
+node-block sparsity pattern, per-cell slot table, external load vector,
+Dirichlet arrays, matrix values (FP64 and/or FP32), preconditioners and the
+Krylov workspaces.  All work is enqueued on torch's current CUDA stream via
+the C ABI; torch is used only for memory and a few O(#dofs) bookkeeping ops.
+"""
+import ctypes as C
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import call, ptr
+from .logger import logger
+
+
+def _stream():
+    return _lib.stream_handle()
+
+
+class DeviceCSR:
+    """Assembled global matrix on the device (scalar CSR values, node-block column indices).
+
+    Stands where the reference passes a PETSc Mat (jax_fem/solver.py:540-553)."""
+
+    def __init__(self, eng, precision, vals, bc_mode):
+        self.eng = eng
+        self.precision = precision
+        self.data = vals
+        self.bc_mode = bc_mode
+        n = eng.num_dofs
+        self.shape = (n, n)
+        self.nnz = eng.nnz
+        self.pc = {}
+
+    @property
+    def dtype(self):
+        return self.data.dtype
+
+    @property
+    def indptr(self):
+        return self.eng.indptr
+
+    @property
+    def indices(self):
+        return self.eng.scalar_indices()
+
+    def matvec(self, x):
+        x = x.to(self.data.dtype).contiguous()
+        y = torch.empty_like(x)
+        call("fem_spmv", C.byref(self.eng.pattern), self.eng.num_nodes, self.eng.vec, self.precision,
+             ptr(self.data), ptr(x), ptr(y), _stream())
+        return y
+
+    __matmul__ = matvec
+
+    def diagonal(self):
+        return self.data[self.eng.diag]
+
+    def preconditioner(self, kind):
+        if kind == _lib.FEM_PC_NONE:
+            return None
+        if kind not in self.pc:
+            n = self.eng.num_dofs if kind == _lib.FEM_PC_JACOBI else self.eng.num_nodes * self.eng.vec ** 2
+            buf = torch.empty(n, dtype=self.data.dtype, device=self.data.device)
+            call("fem_precond_setup", C.byref(self.eng.pattern), self.eng.num_nodes, self.eng.vec, self.precision,
+                 ptr(self.data), kind, ptr(buf), _stream())
+            self.pc[kind] = buf
+        return self.pc[kind]
+
+    def to_torch(self):
+        """torch sparse CSR view (debugging / custom solvers)."""
+        return torch.sparse_csr_tensor(self.indptr, self.indices.to(torch.int64), self.data, size=self.shape)
+
+    def to_scipy(self):
+        """Host copy as scipy CSR (for user code and tests only)."""
+        import scipy.sparse as sp
+        return sp.csr_matrix((self.data.double().cpu().numpy(), self.indices.cpu().numpy(),
+                              self.indptr.cpu().numpy()), shape=self.shape)
+
+
+class Engine:
+    def __init__(self, problem, device="cuda"):
+        if not torch.cuda.is_available():
+            raise RuntimeError("jax_fem_gb300 runs on a CUDA GPU (sm_103a); no GPU is visible")
+        _lib.load()
+        self.problem = problem
+        fe = problem.fes[0]
+        self.fe = fe
+        self.device = torch.device(device)
+        self.vec = fe.vec
+        self.num_nodes = fe.num_total_nodes
+        self.num_cells = fe.num_cells
+        self.num_quads = fe.num_quads
+        self.nn = fe.num_nodes
+        self.num_dofs = self.num_nodes * self.vec
+        self.timing = {"local_assembly": 0.0, "global_matrix": 0.0, "linear": 0.0, "adjoint": 0.0}
+        self.solve_log = []
+        self.sync_timing = True
+        dev = self.device
+        self.coords = torch.as_tensor(fe.points, dtype=torch.float64, device=dev).contiguous()
+        self.conn = torch.as_tensor(fe.cells, dtype=torch.int32, device=dev).contiguous()
+        self.mesh = _lib.FemMesh(fe.elem_id, self.vec, self.num_nodes, self.num_cells,
+                                 self.coords.data_ptr(), self.conn.data_ptr())
+        self._build_pattern()
+        self._bc_seen = None
+        self._mat = None
+        self._mat_key = None
+        self._qp = None
+        self._hist = None
+        self._tangent_cache = {}
+        self._ws = {}
+        self.f_ext = torch.zeros(self.num_dofs, dtype=torch.float64, device=dev)
+        self._loads_done = False
+
+    # ---- pattern -------------------------------------------------------------------
+    def _build_pattern(self):
+        dev, s = self.device, _stream()
+        elem = self.fe.elem_id
+        nb = C.c_size_t()
+        call("fem_pattern_workspace", self.num_cells, self.nn, self.num_nodes, C.byref(nb))
+        ws = torch.empty(nb.value, dtype=torch.uint8, device=dev)
+        self.block_ptr = torch.empty(self.num_nodes + 1, dtype=torch.int64, device=dev)
+        nnzb = C.c_int64()
+        call("fem_pattern_count", elem, ptr(self.conn), self.num_cells, self.num_nodes, ptr(ws), nb.value,
+             ptr(self.block_ptr), C.byref(nnzb), s)
+        self.nnzb = nnzb.value
+        self.block_cols = torch.empty(self.nnzb, dtype=torch.int32, device=dev)
+        call("fem_pattern_fill", elem, ptr(self.conn), self.num_cells, self.num_nodes, ptr(ws), nb.value,
+             ptr(self.block_ptr), ptr(self.block_cols), s)
+        del ws
+        self.slots = torch.empty(self.num_cells * self.nn * self.nn, dtype=torch.uint8, device=dev)
+        call("fem_pattern_slots", elem, ptr(self.conn), self.num_cells, ptr(self.block_ptr), ptr(self.block_cols),
+             ptr(self.slots), s)
+        self.indptr = torch.empty(self.num_dofs + 1, dtype=torch.int64, device=dev)
+        self.diag = torch.empty(self.num_dofs, dtype=torch.int64, device=dev)
+        call("fem_pattern_scalar", self.num_nodes, self.vec, ptr(self.block_ptr), ptr(self.block_cols),
+             ptr(self.indptr), ptr(self.diag), None, s)
+        self.nnz = self.nnzb * self.vec * self.vec
+        self.pattern = _lib.FemPattern(self.nnzb, self.block_ptr.data_ptr(), self.block_cols.data_ptr(),
+                                       self.indptr.data_ptr(), self.diag.data_ptr(), self.slots.data_ptr())
+        self._indices = None
+
+    def scalar_indices(self):
+        if self._indices is None:
+            self._indices = torch.empty(self.nnz, dtype=torch.int32, device=self.device)
+            call("fem_pattern_scalar", self.num_nodes, self.vec, ptr(self.block_ptr), ptr(self.block_cols),
+                 None, None, ptr(self._indices), _stream())
+        return self._indices
+
+    # ---- Dirichlet arrays ---------------------------------------------------------
+    def refresh_bc(self):
+        fe = self.fe
+        key = (fe.bc_version, id(fe.node_inds_list), id(fe.vals_list))
+        if key == self._bc_seen:
+            return
+        rows, vals = [], []
+        for n, v, val in zip(fe.node_inds_list, fe.vec_inds_list, fe.vals_list):
+            rows.append(np.asarray(n, dtype=np.int64) * fe.vec + np.asarray(v, dtype=np.int64))
+            vals.append(np.asarray(val, dtype=np.float64))
+        if rows:
+            rows = np.concatenate(rows)
+            vals = np.concatenate(vals)
+            # later lists overwrite earlier ones on shared rows (solver.py:297-300): keep the last
+            _, last = np.unique(rows[::-1], return_index=True)
+            keep = np.sort(len(rows) - 1 - last)
+            rows, vals = rows[keep], vals[keep]
+        else:
+            rows, vals = np.zeros(0, dtype=np.int64), np.zeros(0)
+        dev = self.device
+        self.bc_rows = torch.as_tensor(rows.astype(np.int32), device=dev)
+        self.bc_rows_long = self.bc_rows.to(torch.int64)
+        self.bc_vals = torch.as_tensor(vals, device=dev)
+        mask = torch.zeros(self.num_dofs, dtype=torch.uint8, device=dev)
+        if len(rows):
+            mask[self.bc_rows_long] = 1
+        self.bc_mask = mask
+        self.n_bc = len(rows)
+        self._bc_seen = key
+        self._tangent_cache.clear()
+
+    # ---- external loads (mass / surface maps independent of u) -----------------------
+    def refresh_loads(self):
+        if self._loads_done:
+            return
+        p = self.problem
+        f = torch.zeros(self.num_dofs, dtype=torch.float64, device=self.device)
+        s = _stream()
+        if p._body_force is not None:
+            fq = torch.as_tensor(p._body_force, dtype=torch.float64, device=self.device).contiguous()
+            call("fem_body_load", C.byref(self.mesh), ptr(fq), ptr(f), s)
+        for bi, t in zip(p.boundary_inds_list, p._surface_tractions):
+            if t is None or len(bi) == 0:
+                continue
+            fc = torch.as_tensor(bi[:, 0].astype(np.int32), device=self.device)
+            fid = torch.as_tensor(bi[:, 1].astype(np.int32), device=self.device)
+            tq = torch.as_tensor(t, dtype=torch.float64, device=self.device).contiguous()
+            call("fem_surface_load", C.byref(self.mesh), ptr(fc), ptr(fid), len(bi), ptr(tq), ptr(f), s)
+        self.f_ext = f
+        self._loads_done = True
+
+    def quad_points(self):
+        x = torch.empty(self.num_cells * self.num_quads * 3, dtype=torch.float64, device=self.device)
+        jxw = torch.empty(self.num_cells * self.num_quads, dtype=torch.float64, device=self.device)
+        call("fem_quad_points", C.byref(self.mesh), ptr(x), ptr(jxw), _stream())
+        return x.reshape(self.num_cells, self.num_quads, 3), jxw.reshape(self.num_cells, self.num_quads)
+
+    def face_quad_points(self, boundary_inds):
+        bi = np.asarray(boundary_inds)
+        nfq = self.fe.num_face_quads
+        x = torch.empty(len(bi) * nfq * 3, dtype=torch.float64, device=self.device)
+        nan = torch.empty(len(bi) * nfq, dtype=torch.float64, device=self.device)
+        if len(bi):
+            fc = torch.as_tensor(bi[:, 0].astype(np.int32), device=self.device)
+            fid = torch.as_tensor(bi[:, 1].astype(np.int32), device=self.device)
+            call("fem_face_quad_points", C.byref(self.mesh), ptr(fc), ptr(fid), len(bi), ptr(x), ptr(nan), _stream())
+        return x.reshape(len(bi), nfq, 3), nan.reshape(len(bi), nfq)
+
+    # ---- material ------------------------------------------------------------------
+    def material(self):
+        p = self.problem
+        if self._mat is None:
+            self._mat = p._resolve_material()
+        m = self._mat
+        key = (p._params_version,)
+        if key != self._mat_key:
+            qp, hist = m.bind(p.internal_vars, self.num_cells, self.num_quads, self.device)
+            same = (self._mat_key is not None and hist is None and getattr(self, "_hist", None) is None and
+                    ((qp is None and self._qp is None) or
+                     (qp is not None and self._qp is not None and torch.equal(qp, self._qp))))
+            consts = m.consts()
+            self._consts = (C.c_double * max(1, len(consts)))(*consts)
+            self._qp, self._hist = qp, hist
+            self._mat_struct = _lib.FemMaterial(m.kind, len(consts), self._consts, m.n_qp_params,
+                                                None if qp is None else qp.data_ptr(),
+                                                None if hist is None else hist.data_ptr())
+            self._mat_key = key
+            if not same:
+                self._tangent_cache.clear()
+        return m, self._mat_struct
+
+    # ---- kernels -------------------------------------------------------------------
+    def residual(self, dofs, apply_bc=True, out=None):
+        """R(u) = R_int(u) + f_ext, BC rows replaced by u_b - g (apply_bc_vec, solver.py:290-304)."""
+        self.refresh_loads()
+        _, ms = self.material()
+        res = out if out is not None else torch.empty(self.num_dofs, dtype=torch.float64, device=self.device)
+        res.copy_(self.f_ext)
+        dofs = dofs.contiguous()
+        call("fem_assemble", C.byref(self.mesh), C.byref(ms), C.byref(self.pattern), _lib.FEM_OUT_RESIDUAL,
+             _lib.FEM_F64, ptr(dofs), None, None, _lib.FEM_BC_NONE, ptr(res), None, None, _stream())
+        if apply_bc:
+            self.refresh_bc()
+            if self.n_bc:
+                call("fem_apply_bc_vec", ptr(res), ptr(dofs), ptr(self.bc_rows), ptr(self.bc_vals), self.n_bc, 1.0,
+                     _stream())
+        return res
+
+    def tangent(self, dofs, precision, bc_mode, cache=True):
+        """Assemble K(u) in `precision` with Dirichlet handling `bc_mode` and unit BC diagonal."""
+        self.refresh_bc()
+        m, ms = self.material()
+        key = (precision, bc_mode)
+        if cache and m.linear and key in self._tangent_cache:
+            return self._tangent_cache[key]
+        dtype = torch.float32 if precision == _lib.FEM_F32 else torch.float64
+        buf_name = f"vals{precision}_{bc_mode}"
+        vals = getattr(self, buf_name, None)
+        if vals is None:
+            vals = torch.empty(self.nnz, dtype=dtype, device=self.device)
+            setattr(self, buf_name, vals)
+        vals.zero_()
+        dofs = dofs.contiguous()
+        call("fem_assemble", C.byref(self.mesh), C.byref(ms), C.byref(self.pattern), _lib.FEM_OUT_MATRIX,
+             precision, ptr(dofs), None, ptr(self.bc_mask), bc_mode, None, ptr(vals), None, _stream())
+        if bc_mode != _lib.FEM_BC_NONE and self.n_bc:
+            call("fem_zero_rows", C.byref(self.pattern), self.vec, precision, ptr(vals), ptr(self.bc_rows), self.n_bc,
+                 1.0, _stream())
+        A = DeviceCSR(self, precision, vals, bc_mode)
+        self._tangent_cache[key] = A
+        return A
+
+    def apply(self, dofs, w, skip_bc_rows=True):
+        """K(u) w in FP64, matrix-free (tangent action kernel)."""
+        self.refresh_bc()
+        _, ms = self.material()
+        out = torch.zeros(self.num_dofs, dtype=torch.float64, device=self.device)
+        call("fem_assemble", C.byref(self.mesh), C.byref(ms), C.byref(self.pattern), _lib.FEM_OUT_APPLY,
+             _lib.FEM_F64, ptr(dofs.contiguous()), ptr(w.contiguous()), ptr(self.bc_mask) if skip_bc_rows else None,
+             _lib.FEM_BC_NONE, None, None, ptr(out), _stream())
+        return out
+
+    def param_vjp(self, dofs, lam):
+        """-lam^T dR/dp per quadrature point (lam masked to 0 on Dirichlet dofs)."""
+        self.refresh_bc()
+        m, ms = self.material()
+        if m.param_index is None:
+            raise NotImplementedError(f"{type(m).__name__} has no differentiable per-point parameter")
+        g = torch.empty(self.num_cells * self.num_quads, dtype=torch.float64, device=self.device)
+        call("fem_param_vjp", C.byref(self.mesh), C.byref(ms), ptr(dofs.contiguous()), ptr(lam.contiguous()),
+             ptr(self.bc_mask), ptr(g), _stream())
+        return g
+
+    def j2_update(self, dofs):
+        m, ms = self.material()
+        out = torch.empty(self.num_cells * self.num_quads * 18, dtype=torch.float64, device=self.device)
+        call("fem_j2_update", C.byref(self.mesh), C.byref(ms), ptr(dofs.contiguous()), ptr(out), _stream())
+        out = out.reshape(self.num_cells, self.num_quads, 18)
+        return out[:, :, :9].reshape(self.num_cells, self.num_quads, 3, 3), \
+            out[:, :, 9:].reshape(self.num_cells, self.num_quads, 3, 3)
+
+    # ---- Krylov --------------------------------------------------------------------
+    def workspace(self, precision):
+        if precision not in self._ws:
+            nb = C.c_size_t()
+            call("fem_krylov_workspace", self.num_dofs, precision, C.byref(nb))
+            self._ws[precision] = torch.empty(nb.value, dtype=torch.uint8, device=self.device)
+        return self._ws[precision]
+
+    def krylov(self, method, A, b, x, pc_kind, rtol, atol, maxiter):
+        """Run fem_pcg / fem_bicgstab; x is updated in place. Returns (iterations, residual norm, status)."""
+        ws = self.workspace(A.precision)
+        pc = A.preconditioner(pc_kind)
+        it, rn, st = C.c_int64(), C.c_double(), C.c_int32()
+        t0 = time.perf_counter()
+        call("fem_pcg" if method == "cg" else "fem_bicgstab", C.byref(self.pattern), self.num_nodes, self.vec,
+             A.precision, ptr(A.data), pc_kind, ptr(pc), ptr(b), ptr(x), float(rtol), float(atol), int(maxiter),
+             ptr(ws), ws.numel(), C.byref(it), C.byref(rn), C.byref(st), _stream())
+        rec = dict(method=method, precision="fp32" if A.precision == _lib.FEM_F32 else "fp64",
+                   iterations=it.value, res_norm=rn.value, status=_lib.SOLVE_STATUS.get(st.value, "?"),
+                   seconds=time.perf_counter() - t0)
+        self.solve_log.append(rec)
+        logger.debug("krylov %s", rec)
+        return it.value, rn.value, st.value
+
+    def cast32(self, x64, mask=None):
+        out = torch.empty(x64.numel(), dtype=torch.float32, device=self.device)
+        call("fem_cast_f64_f32", ptr(x64.contiguous()), ptr(out), x64.numel(), ptr(mask), _stream())
+        return out
+
+    def axpy32(self, alpha, x32, y64):
+        call("fem_axpy_f32_f64", float(alpha), ptr(x32), ptr(y64), y64.numel(), _stream())
+        return y64

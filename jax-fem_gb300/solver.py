@@ -1,0 +1,406 @@
+"""solver(), linear_solver(), get_A(), implicit_vjp() and ad_wrapper() on the GB300 engine.
+
+Mirrors jax_fem/solver.py (Newton branch, 63-553 and 1079-1455):
+
+  * solver_options has the same layout: a 'newton' block (or the legacy flat
+    dict) with tol / rel_tol / line_search_flag / initial_guess and a 'linear'
+    block naming jax_solver / petsc_solver / spsolve_solver / custom_solver.
+    Additional keys: 'precision' ('fp64' default, or 'mixed': FP32 tangent
+    and FP32 Krylov iterations inside FP64 Newton/refinement residuals),
+    'inner_rtol' (mixed inner tolerance), 'max_iter' (Newton cap).
+  * jax_solver -> BiCGStab with jax.scipy's iteration and stopping rule on the
+    row-eliminated matrix (solver.py:63-92), Jacobi if precond.
+  * petsc_solver ksp_type 'cg' -> PCG on the symmetrically eliminated matrix
+    (Dirichlet columns lifted to the right-hand side: same solution as the
+    reference's row elimination because x0 is BC-consistent, solver.py:402-409);
+    other Krylov types -> BiCGStab.  pc_type 'jacobi' -> Jacobi, 'none' -> none,
+    anything else -> 3x3 node-block Jacobi.
+  * spsolve_solver has no direct GPU counterpart here: it is served by
+    block-Jacobi PCG to a relative residual of 1e-12.
+  * amgx_solver is not part of this build (NotImplementedError).
+"""
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .logger import logger
+
+_METHOD_KEYS = frozenset({"newton", "arc_length", "dynamic_relax"})
+_LINEAR_OPTION_KEYS = frozenset({"jax_solver", "amgx_solver", "spsolve_solver", "petsc_solver", "custom_solver"})
+_NEWTON_OPTION_KEYS = frozenset({"tol", "rel_tol", "line_search_flag", "initial_guess", "precision", "inner_rtol",
+                                 "max_iter"})
+
+
+def _resolve_solver_options(solver_options):
+    """solver.py:1088-1106 (same rules) -> ('newton', cfg)."""
+    opts = solver_options or {}
+    methods = [m for m in _METHOD_KEYS if m in opts]
+    if not methods:
+        linear = {k: opts[k] for k in _LINEAR_OPTION_KEYS if k in opts}
+        cfg = {k: opts[k] for k in _NEWTON_OPTION_KEYS if k in opts}
+        if linear:
+            cfg["linear"] = linear
+        return "newton", cfg
+    if len(methods) > 1:
+        raise ValueError(f"Pick one nonlinear method, got {methods}.")
+    method = methods[0]
+    if not isinstance(opts[method], dict):
+        raise ValueError(f"solver_options['{method}'] must be a dict.")
+    return method, opts[method]
+
+
+class LinearSpec:
+    """Resolved linear solver: Krylov method, preconditioner, Dirichlet handling, tolerances."""
+
+    def __init__(self, method, pc, bc_mode, rtol, atol, maxiter, custom=None, options=None):
+        self.method, self.pc, self.bc_mode = method, pc, bc_mode
+        self.rtol, self.atol, self.maxiter = rtol, atol, maxiter
+        self.custom, self.options = custom, options
+
+    def __repr__(self):
+        return f"LinearSpec({self.method}, pc={self.pc}, rtol={self.rtol}, atol={self.atol})"
+
+
+_PC = {"jacobi": _lib.FEM_PC_JACOBI, "none": _lib.FEM_PC_NONE, "bjacobi": _lib.FEM_PC_BJACOBI}
+
+
+def resolve_linear(linear_options):
+    """solver.py:261-284 dispatch rules -> LinearSpec."""
+    lo = linear_options if linear_options is not None else {}
+    if len(lo.keys() & _LINEAR_OPTION_KEYS) == 0:
+        lo["jax_solver"] = {}
+    if "jax_solver" in lo:
+        precond = lo["jax_solver"].get("precond", True)
+        o = lo["jax_solver"]
+        return LinearSpec("bicgstab", _lib.FEM_PC_JACOBI if precond else _lib.FEM_PC_NONE, _lib.FEM_BC_ROWS,
+                          o.get("tol", 1e-10), o.get("atol", 1e-10), o.get("maxiter", 10000))
+    if "amgx_solver" in lo:
+        raise NotImplementedError("amgx_solver is not part of this build (use petsc_solver cg + jacobi/bjacobi)")
+    if "spsolve_solver" in lo:
+        o = lo["spsolve_solver"]
+        return LinearSpec("cg", _lib.FEM_PC_BJACOBI, _lib.FEM_BC_SYMMETRIC, o.get("rtol", 1e-12), o.get("atol", 0.0),
+                          o.get("max_it", 100000))
+    if "petsc_solver" in lo:
+        o = lo["petsc_solver"]
+        ksp = o.get("ksp_type", "bcgsl")
+        pc = o.get("pc_type", "ilu")
+        if ksp == "preonly":
+            raise NotImplementedError("ksp_type 'preonly' (direct factorisation) is not part of this build")
+        method = "cg" if ksp == "cg" else "bicgstab"
+        pck = _PC.get(pc, _lib.FEM_PC_BJACOBI)
+        if pc not in _PC:
+            logger.info("pc_type %r served by 3x3 node-block Jacobi", pc)
+        bc = _lib.FEM_BC_SYMMETRIC if method == "cg" else _lib.FEM_BC_ROWS
+        return LinearSpec(method, pck, bc, o.get("rtol", 1e-5), o.get("atol", 1e-50), o.get("max_it", 10000))
+    if "custom_solver" in lo:
+        return LinearSpec("custom", _lib.FEM_PC_NONE, _lib.FEM_BC_ROWS, 0.0, 0.0, 0, custom=lo["custom_solver"],
+                          options=lo)
+    raise NotImplementedError("Unknown linear solver.")
+
+
+def _precision(cfg):
+    p = cfg.get("precision", "fp64")
+    if p not in ("fp64", "mixed"):
+        raise ValueError("precision must be 'fp64' or 'mixed'")
+    return p
+
+
+def get_A(problem):
+    """solver.py:540-553: tangent at the last newton_update point with PETSc zeroRows
+    semantics (rows := 0, diag := 1, pattern kept), FP64."""
+    eng = problem._engine
+    point = getattr(problem, "_newton_point", None)
+    if point is None:
+        raise RuntimeError("call problem.newton_update(sol_list) first")
+    return eng.tangent(point, _lib.FEM_F64, _lib.FEM_BC_ROWS, cache=False)
+
+
+def linear_solver(A, b, x0, linear_options, precision="fp64", inner_rtol=1e-5):
+    """Solve A x = b on the device (solver.py:261-284).  A is a DeviceCSR; b, x0 FP64 tensors."""
+    spec = resolve_linear(linear_options)
+    eng = A.eng
+    if spec.custom is not None:
+        return spec.custom(A, b, x0, linear_options)
+    x = torch.zeros_like(b) if x0 is None else x0.clone()
+    if A.precision == _lib.FEM_F64:
+        it, rn, st = eng.krylov(spec.method, A, b.contiguous(), x, spec.pc, spec.rtol, spec.atol, spec.maxiter)
+        return x, (it, rn, st)
+    b32 = eng.cast32(b)
+    x32 = eng.cast32(x)
+    it, rn, st = eng.krylov(spec.method, A, b32, x32, spec.pc, inner_rtol, 0.0, spec.maxiter)
+    return x32.double(), (it, rn, st)
+
+
+def _timed(eng, key, t0):
+    if eng.sync_timing:
+        torch.cuda.current_stream().synchronize()
+    eng.timing[key] += time.perf_counter() - t0
+
+
+def _newton_step(problem, eng, dofs, res, spec, precision, cfg):
+    """One Newton correction A inc = -res (solver.py:390-421) with the Dirichlet rows of the
+    increment equal to g - u_b."""
+    prec = _lib.FEM_F32 if precision == "mixed" else _lib.FEM_F64
+    eng.refresh_bc()
+    rows = eng.bc_rows_long
+    du_b = eng.bc_vals - dofs[rows] if eng.n_bc else None
+    t0 = time.perf_counter()
+    if spec.custom is not None:
+        A = eng.tangent(dofs, _lib.FEM_F64, _lib.FEM_BC_ROWS)
+        x0 = torch.zeros_like(dofs)
+        if eng.n_bc:
+            x0[rows] = du_b
+        inc = torch.as_tensor(spec.custom(A, -res, x0, spec.options), dtype=torch.float64, device=dofs.device)
+        eng.timing["linear"] += time.perf_counter() - t0
+        return dofs + inc.reshape(-1)
+    A = eng.tangent(dofs, prec, spec.bc_mode)
+    _timed(eng, "global_matrix", t0)
+    t0 = time.perf_counter()
+    b = -res
+    x0 = torch.zeros_like(dofs)
+    if eng.n_bc:
+        x0[rows] = du_b
+        if spec.bc_mode == _lib.FEM_BC_SYMMETRIC and bool((du_b != 0).any()):
+            # lift the eliminated Dirichlet columns: b_f -= K_fb (g - u_b)
+            b = b - eng.apply(dofs, x0, skip_bc_rows=True)
+        b[rows] = du_b
+    inner = cfg.get("inner_rtol", 1e-5)
+    if prec == _lib.FEM_F64:
+        x = x0.clone()
+        it, rn, st = eng.krylov(spec.method, A, b, x, spec.pc, spec.rtol, spec.atol, spec.maxiter)
+        if spec.method == "bicgstab":
+            err = torch.linalg.norm(A.matvec(x) - b).item()      # solver.py:86-89
+            assert err < 0.1, f"linear solver failed to converge with err = {err}"
+        inc = x
+    else:
+        b32 = eng.cast32(b)
+        x32 = eng.cast32(x0)
+        it, rn, st = eng.krylov(spec.method, A, b32, x32, spec.pc, inner, 0.0, spec.maxiter)
+        inc = None
+    _timed(eng, "linear", t0)
+    if st == _lib.FEM_SOLVE_NAN:
+        raise FloatingPointError("linear solve produced NaN")
+    if cfg.get("line_search_flag", False):
+        if inc is None:
+            inc = x32.double()
+        return _line_search(problem, eng, dofs, inc)
+    if inc is None:
+        new = dofs.clone()
+        eng.axpy32(1.0, x32, new)
+        if eng.n_bc:
+            new[rows] = eng.bc_vals      # constraints hold exactly in FP64
+        return new
+    return dofs + inc
+
+
+def _line_search(problem, eng, dofs, inc):
+    """solver.py:424-463: three step halvings on ||R_bc(u + alpha inc)||."""
+    def norm(alpha):
+        return torch.linalg.norm(eng.residual(dofs + alpha * inc, apply_bc=True)).item()
+
+    alpha = 1.0
+    rn = norm(alpha)
+    for i in range(3):
+        alpha *= 0.5
+        rh = norm(alpha)
+        logger.debug("Line search (step halving): i = %d, alpha = %g, res_norm = %g, res_norm_half = %g",
+                     i, alpha, rn, rh)
+        if rh > rn:
+            alpha *= 2.0
+            break
+        rn = rh
+    return dofs + alpha * inc
+
+
+def solver(problem, solver_options={}):
+    """Newton solve (solver.py:1112-1356).  Returns sol_list = [tensor (num_nodes, vec)] (FP64, device)."""
+    method, cfg = _resolve_solver_options(solver_options)
+    if method != "newton":
+        raise NotImplementedError(f"'{method}' is not part of this build (Newton only)")
+    eng = problem._engine
+    spec = resolve_linear(cfg.get("linear", {}))
+    precision = _precision(cfg)
+    wall0 = time.perf_counter()
+    if "initial_guess" in cfg:
+        ig = cfg["initial_guess"]
+        if isinstance(ig, (list, tuple)):
+            ig = ig[0]
+        dofs = torch.as_tensor(ig, dtype=torch.float64, device=eng.device).detach().reshape(-1).clone()
+    else:
+        dofs = torch.zeros(eng.num_dofs, dtype=torch.float64, device=eng.device)
+    rel_tol = cfg.get("rel_tol", 1e-8)
+    tol = cfg.get("tol", 1e-6)
+    max_iter = cfg.get("max_iter", 200)
+
+    t0 = time.perf_counter()
+    res = eng.residual(dofs, apply_bc=True)
+    res_val = torch.linalg.norm(res).item()
+    _timed(eng, "local_assembly", t0)
+    res0 = res_val
+    rel = res_val / res0 if res0 > 0 else 0.0
+    logger.info("  iter 0: nonlinear residual L2 norm = %.3g (relative to initial = %.3g)", res_val, rel)
+    n_iters = 0
+    while rel > rel_tol and res_val > tol:
+        n_iters += 1
+        if n_iters > max_iter:
+            raise RuntimeError(f"Newton did not converge in {max_iter} iterations (rel res {rel:.3g})")
+        dofs = _newton_step(problem, eng, dofs, res, spec, precision, cfg)
+        t0 = time.perf_counter()
+        res = eng.residual(dofs, apply_bc=True)
+        res_val = torch.linalg.norm(res).item()
+        _timed(eng, "local_assembly", t0)
+        rel = res_val / res0
+        logger.info("  iter %d: nonlinear residual L2 norm = %.3g (relative to initial = %.3g)", n_iters, res_val, rel)
+    if not np.isfinite(res_val):
+        raise FloatingPointError("res_val contains NaN, stop the program!")   # solver.py:1335
+    problem._newton_point = dofs
+    problem.newton_info = dict(iterations=n_iters, res=res_val, res0=res0, rel=rel,
+                               wall=time.perf_counter() - wall0)
+    return problem.unflatten_fn_sol_list(dofs)
+
+
+def _flat_v(v_list, device):
+    if isinstance(v_list, (list, tuple)):
+        v_list = v_list[0]
+    return torch.as_tensor(v_list, dtype=torch.float64, device=device).reshape(-1).contiguous()
+
+
+def adjoint_solve(problem, dofs, v, adjoint_solver_options=None, precision="fp64", inner_rtol=1e-5,
+                  max_refine=30):
+    """lam_f = K_ff^-1 v_f (the free block of A^T lam = v, solver.py:1399-1409).  Dirichlet
+    entries of lam are returned as 0: the parameter VJP never reads them.
+
+    precision 'mixed': FP32 Krylov corrections inside FP64 iterative refinement whose
+    residual v_f - K_ff lam_f is the matrix-free FP64 tangent action; it stops at the
+    linear solver's relative tolerance measured on that FP64 residual."""
+    eng = problem._engine
+    opts = dict(adjoint_solver_options or {})
+    prec_opt = opts.pop("precision", precision)
+    inner_rtol = opts.pop("inner_rtol", inner_rtol)
+    spec = resolve_linear(opts)
+    eng.refresh_bc()
+    b = v.clone()
+    if eng.n_bc:
+        b[eng.bc_rows_long] = 0.0
+    if spec.custom is not None:
+        A = eng.tangent(dofs, _lib.FEM_F64, _lib.FEM_BC_SYMMETRIC)
+        return torch.as_tensor(spec.custom(A, b, None, spec.options), dtype=torch.float64, device=dofs.device)
+    t0 = time.perf_counter()
+    if prec_opt == "fp64":
+        A = eng.tangent(dofs, _lib.FEM_F64, _lib.FEM_BC_SYMMETRIC)
+        lam = torch.zeros_like(b)
+        eng.krylov(spec.method, A, b, lam, spec.pc, spec.rtol, spec.atol, spec.maxiter)
+        _timed(eng, "linear", t0)
+        return lam
+    A = eng.tangent(dofs, _lib.FEM_F32, _lib.FEM_BC_SYMMETRIC)
+    lam = torch.zeros_like(b)
+    r = b
+    bn = torch.linalg.norm(b).item()
+    if bn == 0.0:
+        return lam
+    target = max(spec.rtol * bn, spec.atol)
+    for _ in range(max_refine):
+        r32 = eng.cast32(r, eng.bc_mask)
+        d32 = torch.zeros_like(r32)
+        _, _, st = eng.krylov(spec.method, A, r32, d32, spec.pc, inner_rtol, 0.0, spec.maxiter)
+        if st == _lib.FEM_SOLVE_NAN:
+            raise FloatingPointError("adjoint inner solve produced NaN")
+        eng.axpy32(1.0, d32, lam)
+        if eng.n_bc:
+            lam[eng.bc_rows_long] = 0.0
+        r = b - eng.apply(dofs, lam, skip_bc_rows=True)
+        if eng.n_bc:
+            r[eng.bc_rows_long] = 0.0
+        if torch.linalg.norm(r).item() <= target:
+            break
+    _timed(eng, "linear", t0)
+    return lam
+
+
+def implicit_vjp(problem, sol_list, params, v_list, adjoint_solver_options, precision="fp64"):
+    """solver.py:1362-1418: returns -lam^T dc/dp with c = apply_bc(R(u, set_params(p)))."""
+    eng = problem._engine
+    t0 = time.perf_counter()
+    with torch.no_grad():
+        problem.set_params(params.detach())
+        dofs = _flat_v(sol_list, eng.device)
+        v = _flat_v(v_list, eng.device)
+        lam = adjoint_solve(problem, dofs, v, adjoint_solver_options, precision)
+        g_qp = eng.param_vjp(dofs, lam)
+    m = eng._mat
+    with torch.enable_grad():
+        p = params.detach().clone().requires_grad_(True)
+        problem.set_params(p)
+        iv = problem.internal_vars[m.param_index]
+        if not (torch.is_tensor(iv) and iv.requires_grad):
+            raise RuntimeError("set_params must build internal_vars from params with torch operations so the "
+                               "parameter chain rule can be applied")
+        if iv.numel() == g_qp.numel():
+            go = g_qp.reshape(iv.shape)
+        elif iv.numel() == eng.num_cells:
+            go = g_qp.reshape(eng.num_cells, eng.num_quads).sum(1).reshape(iv.shape)
+        else:
+            raise ValueError("unexpected internal variable shape for the parameter VJP")
+        (g,) = torch.autograd.grad(iv, p, grad_outputs=go.to(iv.dtype), allow_unused=True)
+    with torch.no_grad():
+        problem.set_params(params.detach())
+    eng.timing["adjoint"] += time.perf_counter() - t0
+    if g is None:
+        g = torch.zeros_like(params)
+    return g.to(params.dtype)
+
+
+def ad_wrapper(problem, solver_options={}, adjoint_solver_options={}):
+    """solver.py:1421-1455: differentiable fwd_pred(params) -> sol_list (torch.autograd)."""
+    _, cfg = _resolve_solver_options(solver_options)
+    precision = _precision(cfg)
+
+    class _ForwardPrediction(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, params):
+            problem.set_params(params.detach())
+            sol_list = solver(problem, solver_options)
+            ctx.save_for_backward(params)
+            ctx.sol_list = [s.detach() for s in sol_list]
+            return tuple(sol_list)
+
+        @staticmethod
+        def backward(ctx, *v):
+            (params,) = ctx.saved_tensors
+            logger.info("Running backward and solving the adjoint problem...")
+            return implicit_vjp(problem, ctx.sol_list, params, list(v), adjoint_solver_options, precision)
+
+    def fwd_pred(params):
+        return list(_ForwardPrediction.apply(params))
+
+    return fwd_pred
+
+
+# ---- BC helpers of the reference, device versions (solver.py:290-363) ----------------
+def apply_bc_vec(res_vec, dofs, problem, scale=1.0):
+    eng = problem._engine
+    eng.refresh_bc()
+    res = res_vec.clone().contiguous()
+    if eng.n_bc:
+        res[eng.bc_rows_long] = dofs[eng.bc_rows_long] - eng.bc_vals * scale
+    return res
+
+
+def assign_bc(dofs, problem):
+    eng = problem._engine
+    eng.refresh_bc()
+    out = dofs.clone()
+    if eng.n_bc:
+        out[eng.bc_rows_long] = eng.bc_vals
+    return out
+
+
+def copy_bc(dofs, problem):
+    eng = problem._engine
+    eng.refresh_bc()
+    out = torch.zeros_like(dofs)
+    if eng.n_bc:
+        out[eng.bc_rows_long] = dofs[eng.bc_rows_long]
+    return out

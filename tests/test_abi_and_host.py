@@ -1,0 +1,150 @@
+"""CPU tests: the C-ABI library loads and exports every declared symbol, argument checks
+fail loudly without touching a GPU, and the host-side logic (options, Dirichlet / face
+detection, user-map probing, meshes) matches the reference's rules."""
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import ROOT, golden
+
+
+def _declared():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", f)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(fem_[a-z0-9_]+)\s*\(", src))
+    return names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = _declared()
+    assert len(names) >= 25
+    for n in sorted(names):
+        assert hasattr(lib, n), f"{n} declared in include/ but not exported"
+
+
+def test_signatures_cover_declared(lib):
+    import jax_fem_gb300 as jf
+    assert _declared() == set(jf._lib.SIGNATURES)
+
+
+def test_argument_errors_without_gpu(lib):
+    import ctypes as C
+    import jax_fem_gb300 as jf
+    rc = lib.fem_element_info(99, None, None, None, None)
+    assert rc == jf._lib.FEM_ERR_ARG
+    assert "unknown element" in jf._lib.last_error()
+    nb = C.c_size_t()
+    jf._lib.call("fem_krylov_workspace", 1000, jf._lib.FEM_F32, C.byref(nb))
+    assert nb.value > 8 * 4000
+    with pytest.raises(jf._lib.FemError):
+        jf._lib.call("fem_krylov_workspace", -1, jf._lib.FEM_F32, C.byref(nb))
+    assert lib.fem_version() >= 100
+
+
+def test_element_tables_match_oracle(lib):
+    from jax_fem_gb300 import basis
+    from oracle import basis as ob
+    for e in ("HEX8", "TET10"):
+        t, o = basis.element_tables(e), ob.element_tables(e)
+        for k in ("shape_vals", "shape_grads_ref", "quad_weights", "face_shape_vals", "face_shape_grads_ref",
+                  "face_quad_weights", "face_normals", "face_inds"):
+            np.testing.assert_allclose(t[k], o[k], atol=1e-14)
+        # quadrature exactness: weights sum to the reference volume, shape functions partition unity
+        assert abs(t["quad_weights"].sum() - (1.0 if e == "HEX8" else 1.0 / 6.0)) < 1e-15
+        np.testing.assert_allclose(t["shape_vals"].sum(1), 1.0, atol=1e-14)
+        np.testing.assert_allclose(t["shape_grads_ref"].sum(1), 0.0, atol=1e-13)
+
+
+def test_resolve_solver_options_rules(lib):
+    import importlib
+    S = importlib.import_module("jax_fem_gb300.solver")
+    assert S._resolve_solver_options({}) == ("newton", {})
+    m, cfg = S._resolve_solver_options({"petsc_solver": {}, "tol": 1e-5})
+    assert m == "newton" and cfg == {"linear": {"petsc_solver": {}}, "tol": 1e-5}
+    with pytest.raises(ValueError):
+        S._resolve_solver_options({"newton": {}, "arc_length": {}})
+    with pytest.raises(ValueError):
+        S._resolve_solver_options({"newton": 3})
+    spec = S.resolve_linear({})
+    assert spec.method == "bicgstab" and spec.rtol == 1e-10 and spec.atol == 1e-10 and spec.maxiter == 10000
+    spec = S.resolve_linear({"petsc_solver": {"ksp_type": "cg", "pc_type": "jacobi"}})
+    assert spec.method == "cg" and spec.rtol == 1e-5
+    with pytest.raises(NotImplementedError):
+        S.resolve_linear({"amgx_solver": {}})
+
+
+def test_dirichlet_and_faces_match_oracle(lib):
+    from jax_fem_gb300.fe import FiniteElement
+    from jax_fem_gb300.generate_mesh import Mesh
+    from oracle import fem as ofem
+    g = golden("plasticity")
+    top = lambda p: np.isclose(p[2], 10.0, atol=1e-5)
+    bottom = lambda p: np.isclose(p[2], 0.0, atol=1e-5)
+    both = lambda p, i: np.logical_and(np.isclose(p[2], 0.0, atol=1e-5), i % 2 == 0)
+    bc = [[bottom, top, both], [0, 2, 1], [lambda p: 0.0, lambda p: 0.1 * p[0], lambda p: 2.0]]
+    fe = FiniteElement(Mesh(g["points"], g["cells"]), 3, 3, "HEX8", dirichlet_bc_info=bc)
+    ofe = ofem.OracleFE(g["points"], g["cells"], 3, "HEX8", dirichlet_bc_info=bc)
+    for a, b in zip(fe.node_inds_list, ofe.node_inds_list):
+        np.testing.assert_array_equal(a, b)
+    for a, b in zip(fe.vals_list, ofe.vals_list):
+        np.testing.assert_allclose(a, b, rtol=0, atol=0)
+    for a, b in zip(fe.get_boundary_conditions_inds([top, bottom]), ofe.get_boundary_conditions_inds([top, bottom])):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_probe_tensor_map(lib):
+    import jax_fem_gb300 as jf
+    from jax_fem_gb300.materials import probe_tensor_map
+
+    def elastic(u_grad):
+        E, nu = 70e3, 0.3
+        mu = E / (2 * (1 + nu))
+        lm = E * nu / ((1 + nu) * (1 - 2 * nu))
+        eps = 0.5 * (u_grad + u_grad.T)
+        return lm * np.trace(eps) * np.eye(3) + 2 * mu * eps
+
+    m = probe_tensor_map(elastic, 3)
+    assert isinstance(m, jf.LinearElastic)
+    assert abs(m.E - 70e3) < 1e-9 and abs(m.nu - 0.3) < 1e-14
+    assert isinstance(probe_tensor_map(lambda x: x, 1), jf.Laplace)
+    aniso = np.diag([1.0, 2.0, 3.0])
+    assert isinstance(probe_tensor_map(lambda g: (aniso @ g.T).T, 1), jf.GeneralLinear)
+    with pytest.raises(NotImplementedError):
+        probe_tensor_map(lambda g: g ** 3, 3)
+    with pytest.raises(NotImplementedError):
+        probe_tensor_map(lambda g, theta: g * theta, 3)
+
+
+def test_box_meshes(lib):
+    import jax_fem_gb300 as jf
+    from oracle import fem as ofem
+    m = jf.box_mesh(3, 4, 5, 1.0, 2.0, 3.0)
+    p, c = ofem.box_mesh(3, 4, 5, 1.0, 2.0, 3.0)
+    np.testing.assert_array_equal(m.points, p)
+    np.testing.assert_array_equal(m.cells_dict["hexahedron"], c)
+    t = jf.box_mesh_tet10(2, 2, 2, 1.0, 1.0, 1.0)
+    pts, cells = t.points, t.cells_dict["tetra10"]
+    assert cells.shape == (48, 10) and len(pts) == 27 + 98
+    P = pts[cells]
+    vol = np.einsum("ij,ij->i", np.cross(P[:, 1] - P[:, 0], P[:, 2] - P[:, 0]), P[:, 3] - P[:, 0]) / 6
+    assert np.all(vol > 0) and abs(vol.sum() - 1.0) < 1e-12
+    # midpoints lie halfway along their edges
+    for k, (a, b) in enumerate([(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]):
+        np.testing.assert_allclose(P[:, 4 + k], 0.5 * (P[:, a] + P[:, b]), atol=1e-15)
+
+
+def test_pointwise_eval_falls_back(lib):
+    from jax_fem_gb300.fe import eval_pointwise
+    x = np.random.default_rng(0).standard_normal((20, 3))
+    f1 = lambda p: np.linalg.norm(p)                    # not vectorisable by axis trick
+    np.testing.assert_allclose(eval_pointwise(f1, [x]), np.linalg.norm(x, axis=1))
+    f2 = lambda p: -np.array([1e3 * p[0], 2e3 * p[1], 3e3 * p[2]])
+    np.testing.assert_allclose(eval_pointwise(f2, [x], (3,)), -x * np.array([1e3, 2e3, 3e3]))
+    f3 = lambda p: np.array([0.0, 10.0, 10.0])
+    assert eval_pointwise(f3, [x], (3,)).shape == (20, 3)

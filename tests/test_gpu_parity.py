@@ -1,0 +1,340 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the CPU oracle and the
+reference's FEniCSx gold fixtures.  Tolerances are stated per test."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _cube(cuda):
+    import cases
+    return cases.cube_elasticity(golden("linear_elasticity_cube"))
+
+
+def test_pattern_bit_exact(cuda):
+    """CSR pattern (indptr/indices after coalescing) equals the PETSc COO pattern of I/J."""
+    from oracle import fem as ofem
+    prob, oprob = _cube(cuda)
+    eng = prob._engine
+    ip, ix = ofem.coo_pattern(oprob.I, oprob.J, oprob.num_total_dofs_all_vars)
+    assert eng.nnz == len(ix) == 268119
+    np.testing.assert_array_equal(eng.indptr.cpu().numpy(), ip)
+    np.testing.assert_array_equal(eng.scalar_indices().cpu().numpy(), ix)
+
+
+def test_assembled_values_fp64(cuda):
+    """get_A after newton_update: PETSc zeroRows semantics, values within 1e-12 relative."""
+    import jax_fem_gb300 as jf
+    from oracle import fem as ofem
+    prob, oprob = _cube(cuda)
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal(oprob.num_total_dofs_all_vars) * 1e-3
+    prob.newton_update([torch.tensor(u, device=cuda).reshape(-1, 3)])
+    A = jf.get_A(prob)
+    oprob.newton_update(torch.tensor(u))
+    Ao = ofem.assemble_petsc(oprob)
+    a = A.data.cpu().numpy()
+    scale = np.abs(Ao.data).max()
+    assert np.abs(a - Ao.data).max() <= 1e-12 * scale
+    np.testing.assert_array_equal(A.indices.cpu().numpy(), Ao.indices)
+
+
+def test_assembled_values_fp32(cuda):
+    import jax_fem_gb300 as jf
+    from oracle import fem as ofem
+    prob, oprob = _cube(cuda)
+    eng = prob._engine
+    A32 = eng.tangent(torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda), jf._lib.FEM_F32,
+                      jf._lib.FEM_BC_ROWS, cache=False)
+    oprob.newton_update(torch.zeros(oprob.num_total_dofs_all_vars))
+    Ao = ofem.assemble_petsc(oprob)
+    scale = np.abs(Ao.data).max()
+    assert np.abs(A32.data.double().cpu().numpy() - Ao.data).max() <= 2e-6 * scale
+
+
+def test_residual_matches_oracle(cuda):
+    prob, oprob = _cube(cuda)
+    rng = np.random.default_rng(5)
+    u = rng.standard_normal(oprob.num_total_dofs_all_vars) * 1e-3
+    r = prob.compute_residual([torch.tensor(u, device=cuda).reshape(-1, 3)])[0].reshape(-1).cpu().numpy()
+    ro = oprob.compute_residual(torch.tensor(u)).numpy()
+    assert np.abs(r - ro).max() <= 1e-12 * np.abs(ro).max()
+
+
+def test_spmv_matches_scipy(cuda):
+    import jax_fem_gb300 as jf
+    from oracle import fem as ofem
+    prob, oprob = _cube(cuda)
+    eng = prob._engine
+    A = eng.tangent(torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda), jf._lib.FEM_F64,
+                    jf._lib.FEM_BC_ROWS, cache=False)
+    oprob.newton_update(torch.zeros(oprob.num_total_dofs_all_vars))
+    Ao = ofem.assemble_petsc(oprob)
+    x = np.random.default_rng(1).standard_normal(Ao.shape[0])
+    y = A.matvec(torch.tensor(x, device=cuda)).cpu().numpy()
+    yo = Ao @ x
+    assert np.abs(y - yo).max() <= 1e-12 * np.abs(yo).max()
+    A32 = eng.tangent(torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda), jf._lib.FEM_F32,
+                      jf._lib.FEM_BC_ROWS, cache=False)
+    y32 = A32.matvec(torch.tensor(x, device=cuda)).double().cpu().numpy()
+    assert np.abs(y32 - yo).max() <= 1e-5 * np.abs(yo).max()
+
+
+def test_cube_solution_gold_and_oracle(cuda):
+    """test_linear_elasticity_cube.py:73-83 (decimal 5) and the oracle's direct solve (1e-10)."""
+    import jax_fem_gb300 as jf
+    from oracle import solve as osolve
+    g = golden("linear_elasticity_cube")
+    prob, oprob = _cube(cuda)
+    sol = jf.solver(prob)[0].cpu().numpy()                       # default: jax_solver (BiCGStab + Jacobi)
+    np.testing.assert_array_almost_equal(g["sol"], sol, decimal=5)
+    osol = osolve.newton_solve(oprob, {"spsolve_solver": {}})
+    sol_cg = jf.solver(prob, {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-13}})[0]
+    assert np.abs(sol_cg.cpu().numpy() - osol).max() <= 1e-10 * np.abs(osol).max()
+    assert np.abs(sol - osol).max() <= 1e-7 * np.abs(osol).max()
+
+
+def test_bicgstab_matches_jax_iteration(cuda):
+    """fem_bicgstab follows jax.scipy's BiCGStab: same iteration count and iterate as the restated loop."""
+    import jax_fem_gb300 as jf
+    from oracle import fem as ofem, solve as osolve
+    prob, oprob = _cube(cuda)
+    eng = prob._engine
+    z = torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda)
+    res = eng.residual(z, apply_bc=True)
+    A = eng.tangent(z, jf._lib.FEM_F64, jf._lib.FEM_BC_ROWS, cache=False)
+    b = -res
+    oprob.newton_update(torch.zeros(oprob.num_total_dofs_all_vars))
+    Ao = ofem.assemble_petsc(oprob)
+    bo = b.cpu().numpy()
+    d = Ao.diagonal()
+    # same iterate after a fixed number of steps (before rounding differences grow)
+    for k in (1, 2, 10):
+        x = torch.zeros_like(b)
+        it, rn, st = eng.krylov("bicgstab", A, b, x, jf._lib.FEM_PC_JACOBI, 1e-10, 1e-10, k)
+        xo, ito = osolve.bicgstab_jax(Ao, bo, None, lambda v: v / d, 1e-10, 1e-10, k)
+        assert it == ito == k and st == jf._lib.FEM_SOLVE_MAXITER
+        assert np.abs(x.cpu().numpy() - xo).max() <= 1e-9 * np.abs(xo).max()
+    # full solve: same stopping rule, iteration counts within rounding drift
+    x = torch.zeros_like(b)
+    it, rn, st = eng.krylov("bicgstab", A, b, x, jf._lib.FEM_PC_JACOBI, 1e-10, 1e-10, 10000)
+    xo, ito = osolve.bicgstab_jax(Ao, bo, None, lambda v: v / d, 1e-10, 1e-10, 10000)
+    assert st == 0 and abs(it - ito) <= max(3, 0.1 * ito)
+    assert rn <= 1e-10 * np.linalg.norm(bo) * (1 + 1e-12)
+    assert np.abs(x.cpu().numpy() - xo).max() <= 1e-6 * np.abs(xo).max()
+
+
+def test_poisson_gold(cuda):
+    import cases
+    import jax_fem_gb300 as jf
+    g = golden("linear_poisson")
+    prob, _ = cases.poisson(g)
+    sol = jf.solver(prob)[0].cpu().numpy()
+    np.testing.assert_array_almost_equal(g["sol"], sol, decimal=5)
+
+
+def test_cylinder_gold_and_area(cuda):
+    """test_linear_elasticity_cylinder.py:113-132: decimal 3 solution, decimal 4 area."""
+    import cases
+    import jax_fem_gb300 as jf
+    g = golden("linear_elasticity_cylinder")
+    prob, _ = cases.cylinder_elasticity(g)
+    sol = jf.solver(prob, {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}})[0]
+    np.testing.assert_array_almost_equal(g["sol"], sol.cpu().numpy(), decimal=3)
+    _, nanson = prob._engine.face_quad_points(prob.boundary_inds_list[0])
+    np.testing.assert_almost_equal(g["surface_area"][0], nanson.sum().item(), decimal=4)
+
+
+def test_hyperelastic_gold_and_traction(cuda):
+    """test_hyper_elasticity.py:109-127: decimal 5 solution and top traction."""
+    import cases
+    import jax_fem_gb300 as jf
+    g = golden("hyperelasticity")
+    prob, _, _ = cases.hyperelastic(g)
+    sol = jf.solver(prob, {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}})[0]
+    np.testing.assert_array_almost_equal(g["sol"], sol.cpu().numpy(), decimal=5)
+    fe = prob.fes[0]
+    top = fe.get_boundary_conditions_inds([cases._top])[0]
+    fg, nanson = fe.get_face_shape_grads(top)
+    cells = torch.as_tensor(fe.cells, device=cuda)[torch.as_tensor(top[:, 0], device=cuda)]
+    ug = torch.einsum("fnv,fqnd->fqvd", sol[cells], fg)
+    F = ug + torch.eye(3, dtype=torch.float64, device=cuda)
+    E, nu = 1e3, 0.3
+    mu, kappa = E / (2 * (1 + nu)), E / (3 * (1 - 2 * nu))
+    J = torch.linalg.det(F)
+    H = torch.linalg.inv(F).transpose(-1, -2)
+    I1 = (F * F).sum((-1, -2))
+    P = mu * J[..., None, None] ** (-2 / 3) * (F - I1[..., None, None] / 3 * H) + kappa * (J * (J - 1))[..., None, None] * H
+    trac = (P[..., :, 2] * nanson[..., None]).sum((0, 1))
+    np.testing.assert_almost_equal(g["traction"][0], trac[2].item(), decimal=5)
+
+
+def test_plasticity_gold(cuda):
+    """test_plasticity.py:129-161: 5 load steps, decimal 5 solution and decimal 3 averaged stress."""
+    import cases
+    import jax_fem_gb300 as jf
+    g = golden("plasticity")
+    prob, bc, disps = cases.plasticity(g)
+    avg = []
+    sol = None
+    for d in disps:
+        bc[2][-1] = (lambda p, d=d: d)
+        prob.fes[0].update_Dirichlet_boundary_conditions(bc)
+        sol = jf.solver(prob, {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}})[0]
+        prob.update_stress_strain(sol)
+        avg.append(prob.compute_avg_stress()[2, 2].item())
+    np.testing.assert_array_almost_equal(g["sol"], sol.cpu().numpy(), decimal=5)
+    np.testing.assert_array_almost_equal(g["avg_stresses"], np.array(avg), decimal=3)
+
+
+def _simp_grad(prob, theta_np, cuda, opts, adj):
+    import jax_fem_gb300 as jf
+    theta = torch.tensor(theta_np, device=cuda, requires_grad=True)
+    fwd = jf.ad_wrapper(prob, opts, adj)
+    sol = fwd(theta)[0]
+    J = torch.dot(prob._engine.f_ext, sol.reshape(-1))
+    J.backward()
+    return sol.detach(), J.item(), theta.grad.detach().cpu().numpy()
+
+
+def test_simp_adjoint_vs_oracle_and_fd(cuda):
+    """ad_wrapper gradient vs the oracle's implicit_vjp (torch AD through the restated residual)
+    within 1e-9 relative, and vs central finite differences (h=1e-6) within 1e-5 relative."""
+    import cases
+    from oracle import solve as osolve
+    prob, oprob, theta_np = cases.simp_box(6, 3, 2)
+    opts = {"petsc_solver": {"ksp_type": "cg", "pc_type": "jacobi", "rtol": 1e-13}}
+    sol, J, g = _simp_grad(prob, theta_np, cuda, opts, opts)
+    oprob.internal_vars = cases.oracle_set_params(oprob, torch.tensor(theta_np))
+    osol = osolve.newton_solve(oprob, {"spsolve_solver": {}})
+    f = prob._engine.f_ext.cpu().numpy()
+    assert np.abs(sol.cpu().numpy() - osol).max() <= 1e-10 * np.abs(osol).max()
+    fo = f.copy()
+    fo[oprob.bc_rows()[0]] = 0.0
+    g_or, _ = osolve.implicit_vjp(oprob, osol, theta_np, cases.oracle_set_params, fo)
+    assert np.abs(g - g_or).max() <= 1e-9 * np.abs(g_or).max()
+    import jax_fem_gb300 as jf
+    rng = np.random.default_rng(0)
+    h = 1e-6
+    for c in rng.choice(len(theta_np), size=5, replace=False):
+        vals = []
+        for s in (+1, -1):
+            tp = theta_np.copy()
+            tp[c, 0] += s * h
+            prob.set_params(torch.tensor(tp, device=cuda))
+            u = jf.solver(prob, opts)[0]
+            vals.append(torch.dot(prob._engine.f_ext, u.reshape(-1)).item())
+        fd = (vals[0] - vals[1]) / (2 * h)
+        assert abs(fd - g[c, 0]) <= 1e-5 * np.abs(g).max()
+
+
+def test_mixed_precision_matches_fp64(cuda):
+    """Mixed (FP32 tangent + FP32 PCG in FP64 refinement) vs FP64: solution, objective, gradient."""
+    import cases
+    prob, _, theta_np = cases.simp_box(12, 6, 3)
+    o64 = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}, "rel_tol": 1e-12, "tol": 0.0}
+    omx = dict(o64, precision="mixed")
+    a64 = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}}
+    amx = dict(a64, precision="mixed")
+    s64, J64, g64 = _simp_grad(prob, theta_np, cuda, o64, a64)
+    smx, Jmx, gmx = _simp_grad(prob, theta_np, cuda, omx, amx)
+    assert (smx - s64).abs().max().item() <= 1e-9 * s64.abs().max().item()
+    assert abs(Jmx - J64) <= 1e-10 * abs(J64)
+    assert np.abs(gmx - g64).max() <= 1e-8 * np.abs(g64).max()
+
+
+def test_tet10_pattern_and_values(cuda):
+    """TET10 (Kuhn split) pattern bit-exact and FP64 tangent within 1e-12 of the oracle."""
+    import jax_fem_gb300 as jf
+    from oracle import fem as ofem, materials as omat
+    m = jf.box_mesh_tet10(3, 2, 2, 1.0, 1.0, 1.0)
+    pts, cells = m.points, m.cells_dict["tetra10"]
+    left = lambda p: np.isclose(p[0], 0.0, atol=1e-5)
+    bc = [[left] * 3, [0, 1, 2], [lambda p: 0.0] * 3]
+
+    class P(jf.Problem):
+        def get_tensor_map(self):
+            return jf.LinearElastic(1.0, 0.3)
+
+    prob = P(jf.Mesh(pts, cells), vec=3, dim=3, ele_type="TET10", dirichlet_bc_info=bc)
+    oprob = ofem.OracleProblem(pts, cells, 3, ele_type="TET10", dirichlet_bc_info=bc,
+                               tensor_map=omat.linear_elastic(1.0, 0.3))
+    eng = prob._engine
+    ip, ix = ofem.coo_pattern(oprob.I, oprob.J, oprob.num_total_dofs_all_vars)
+    np.testing.assert_array_equal(eng.indptr.cpu().numpy(), ip)
+    np.testing.assert_array_equal(eng.scalar_indices().cpu().numpy(), ix)
+    u = np.random.default_rng(2).standard_normal(oprob.num_total_dofs_all_vars) * 1e-2
+    prob.newton_update([torch.tensor(u, device=cuda).reshape(-1, 3)])
+    A = jf.get_A(prob)
+    oprob.newton_update(torch.tensor(u))
+    Ao = ofem.assemble_petsc(oprob)
+    assert np.abs(A.data.cpu().numpy() - Ao.data).max() <= 1e-12 * np.abs(Ao.data).max()
+
+
+def test_neo_hookean_tangent_matches_ad(cuda):
+    """Hand-derived Neo-Hookean tangent vs the oracle's jacfwd(grad psi) at a deformed state (1e-11)."""
+    import cases
+    import jax_fem_gb300 as jf
+    from oracle import fem as ofem
+    g = golden("hyperelasticity")
+    prob, oprob, _ = cases.hyperelastic(g)
+    u = np.random.default_rng(4).standard_normal(oprob.num_total_dofs_all_vars) * 5e-2
+    prob.newton_update([torch.tensor(u, device=cuda).reshape(-1, 3)])
+    A = jf.get_A(prob)
+    oprob.newton_update(torch.tensor(u))
+    Ao = ofem.assemble_petsc(oprob)
+    assert np.abs(A.data.cpu().numpy() - Ao.data).max() <= 1e-11 * np.abs(Ao.data).max()
+
+
+def test_j2_tangent_matches_ad(cuda):
+    """J2 consistent tangent (plastic branch active) vs the oracle's jacfwd of the return map."""
+    import cases
+    import jax_fem_gb300 as jf
+    from oracle import fem as ofem, materials as omat
+    g = golden("plasticity")
+    prob, bc, disps = cases.plasticity(g)
+    rng = np.random.default_rng(6)
+    C, nq = prob.num_cells, prob.fes[0].num_quads
+    sig = rng.standard_normal((C, nq, 3, 3)) * 100.0
+    sig = 0.5 * (sig + np.swapaxes(sig, -1, -2))
+    eps = rng.standard_normal((C, nq, 3, 3)) * 1e-3
+    eps = 0.5 * (eps + np.swapaxes(eps, -1, -2))
+    prob.internal_vars = [torch.tensor(sig, device=cuda), torch.tensor(eps, device=cuda)]
+    u = rng.standard_normal(prob.num_total_dofs_all_vars) * 1e-2
+    prob.newton_update([torch.tensor(u, device=cuda).reshape(-1, 3)])
+    A = jf.get_A(prob)
+    _, rmap = omat.j2_maps(70e3, 0.3, 250.0)
+    oprob = ofem.OracleProblem(g["points"], g["cells"], 3, dirichlet_bc_info=bc, tensor_map=rmap)
+    oprob.internal_vars = [torch.tensor(sig), torch.tensor(eps)]
+    oprob.newton_update(torch.tensor(u))
+    Ao = ofem.assemble_petsc(oprob)
+    assert np.abs(A.data.cpu().numpy() - Ao.data).max() <= 1e-10 * np.abs(Ao.data).max()
+
+
+def test_nan_input_is_reported(cuda):
+    """A NaN design variable (host-made fault) ends the solve with an error, not a hang."""
+    import cases
+    import jax_fem_gb300 as jf
+    prob, _, theta_np = cases.simp_box(4, 2, 2)
+    theta_np = theta_np.copy()
+    theta_np[3, 0] = np.nan
+    prob.set_params(torch.tensor(theta_np, device=cuda))
+    with pytest.raises((FloatingPointError, AssertionError, RuntimeError)):
+        jf.solver(prob, {"petsc_solver": {"ksp_type": "cg", "pc_type": "jacobi", "rtol": 1e-10}})
+
+
+def test_maxiter_status(cuda):
+    import cases
+    import jax_fem_gb300 as jf
+    prob, _, theta_np = cases.simp_box(8, 4, 2)
+    prob.set_params(torch.tensor(theta_np, device=cuda))
+    eng = prob._engine
+    z = torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda)
+    A = eng.tangent(z, jf._lib.FEM_F64, jf._lib.FEM_BC_SYMMETRIC)
+    b = -eng.residual(z)
+    x = torch.zeros_like(b)
+    it, rn, st = eng.krylov("cg", A, b, x, jf._lib.FEM_PC_JACOBI, 1e-14, 0.0, 3)
+    assert it == 3 and st == jf._lib.FEM_SOLVE_MAXITER
