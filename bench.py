@@ -1,0 +1,412 @@
+"""Benchmark: one SIMP topology-optimisation iteration (assemble + solve + adjoint gradient).
+
+Workload (metric "assemble+solve+adjoint s/iter at 3M DOF: mixed vs FP64 on GB300 @1e-8"):
+HEX8 cantilever 200x100x50 on [0,2]x[0,1]x[0,0.5] (1,000,000 cells, 1,035,351 nodes,
+3,106,053 dofs, CSR nnz 245,844,459), clamped at x=0, traction (0,0,1) on x=2 as the
+surface map, SIMP E = 1e-3 + (1 - 1e-3) theta^3, nu = 0.3, theta = 0.5 + U(-0.05, 0.05)
+(torch.Generator seed 0).  One step = fwd_pred(theta) through ad_wrapper (Newton with PCG
+to relative residual 1e-8), compliance J = f.u, J.backward() (adjoint solve + parameter VJP).
+
+value   : mixed precision (FP32 tangent + FP32 block-Jacobi PCG inside FP64 refinement), s/iter,
+          inputs resident in HBM, CUDA events over exactly K steps.
+fp64    : the same iteration in plain FP64 (FP64 tangent, FP64 PCG), reported beside it.
+e2e     : the mixed iteration through the public API from pinned host theta to host J and
+          gradient, copies inside the timed region.
+roofline: FP32 SpMV (the dominant kernel), CUDA-event timed on the launching stream.
+--impl reference: the FP64 CPU restatement (oracle) of the same iteration on the host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "assemble+solve+adjoint s/iter at 3M DOF: mixed vs FP64 on GB300 @1e-8; HBM GB/s"
+UNIT = "s/iter"
+DEFAULT_SIZE = (200, 100, 50)
+L = (2.0, 1.0, 0.5)
+RTOL = 1e-8
+# FP64 Jacobi-PCG iterations (forward, adjoint) that the full 200x100x50 workload needs to reach
+# RTOL; measured by this bench on a GB300 (printed as fp64.pcg_iterations) and used only to scale
+# the bounded CPU-baseline sample to a full iteration.
+FULL_SIZE_PCG_ITERS = None
+
+
+def workload_name(n):
+    nx, ny, nz = n
+    cells = nx * ny * nz
+    nodes = (nx + 1) * (ny + 1) * (nz + 1)
+    nnz = 9 * (3 * nx + 1) * (3 * ny + 1) * (3 * nz + 1)
+    return (f"SIMP compliance TO iteration, HEX8 cantilever {nx}x{ny}x{nz} ({cells:,} cells, "
+            f"{3 * nodes:,} dofs, CSR nnz {nnz:,})"), cells, nodes, nnz
+
+
+def theta_init(ncells, seed=0):
+    import torch
+    g = torch.Generator().manual_seed(seed)
+    return (0.5 + (torch.rand(ncells, 1, generator=g, dtype=torch.float64) - 0.5) * 0.1)
+
+
+def make_problem(n):
+    import jax_fem_gb300 as jf
+    Lx, Ly, Lz = L
+    m = jf.box_mesh(*n, Lx, Ly, Lz)
+    mesh = jf.Mesh(m.points, m.cells_dict["hexahedron"])
+    left = lambda p: np.isclose(p[0], 0.0, atol=1e-5)
+    right = lambda p: np.isclose(p[0], Lx, atol=1e-5)
+    zero = lambda p: 0.0
+
+    class Cantilever(jf.Problem):
+        def get_tensor_map(self):
+            return jf.SIMPElastic(1.0, 1e-3, 0.3, 3.0)
+
+        def get_surface_maps(self):
+            return [lambda u, x: np.array([0.0, 0.0, 1.0])]
+
+        def set_params(self, params):
+            self.internal_vars = [params[:, None, :].expand(-1, 8, -1)]
+
+    return Cantilever(mesh, vec=3, dim=3, dirichlet_bc_info=[[left] * 3, [0, 1, 2], [zero] * 3],
+                      location_fns=[right])
+
+
+def options(precision):
+    lin = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": RTOL if precision == "fp64" else RTOL}}
+    fwd = dict(lin, rel_tol=RTOL, tol=0.0, precision=precision, inner_rtol=1e-4)
+    adj = dict(lin, precision=precision, inner_rtol=1e-4)
+    return fwd, adj
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = [nm for k, nm in enumerate(names) if any(s[3 + k].lower().startswith("active") for s in self.samples)]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def run_steps(prob, fwd, theta, J_out=None):
+    """One TO iteration through the public API: fwd_pred, compliance, backward."""
+    import torch
+    th = theta.detach().requires_grad_(True)
+    sol = fwd(th)[0]
+    J = torch.dot(prob._engine.f_ext, sol.reshape(-1))
+    J.backward()
+    return J.detach(), th.grad, sol.detach()
+
+
+def spmv_roofline(prob, peak):
+    """Time the FP32 SpMV (mixed path) and the FP64 SpMV with CUDA events on the launching stream."""
+    import torch
+    import jax_fem_gb300 as jf
+    eng = prob._engine
+    out = {}
+    n, nnz, nnzb = eng.num_dofs, eng.nnz, eng.nnzb
+    for prec, es, name in ((jf._lib.FEM_F32, 4, "fp32"), (jf._lib.FEM_F64, 8, "fp64")):
+        A = eng._tangent_cache.get((prec, jf._lib.FEM_BC_SYMMETRIC))
+        if A is None:
+            continue
+        x = torch.randn(n, dtype=A.data.dtype, device="cuda")
+        for _ in range(3):
+            A.matvec(x)
+        s = torch.cuda.current_stream()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        reps = 20
+        torch.cuda.synchronize()
+        ev[0].record(s)
+        for _ in range(reps):
+            A.matvec(x)
+        ev[1].record(s)
+        torch.cuda.synchronize()
+        t = ev[0].elapsed_time(ev[1]) / 1e3 / reps
+        algo = nnz * es + nnzb * 4 + (eng.num_nodes + 1) * 8 + 2 * n * es
+        out[name] = {"seconds": t, "algorithmic_bytes": algo, "achieved_gbs": algo / t / 1e9,
+                     "frac": algo / t / 1e9 / peak}
+    return out
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile(n_units):
+    """DRAM bytes per SpMV launch from the committed ncu summary, scaled to this workload's nnz."""
+    p = os.path.join(ROOT, "profiles", "spmv_fp32_traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d["dram_bytes_per_launch"] * n_units / d["nnz"]
+    except (OSError, KeyError, ValueError, ZeroDivisionError):
+        return None
+
+
+def cpu_baseline(n, iters_full, seconds_budget=20.0):
+    """Time the oracle (numpy/scipy FP64) on a bounded sample and scale to the full workload."""
+    import torch
+    from oracle import fem as ofem, simp_fast
+    sample = (40, 20, 10)
+    pts, cells = ofem.box_mesh(*sample, *L)
+    N = 3 * len(pts)
+    left = np.isclose(pts[:, 0], 0.0, atol=1e-5)
+    bc_rows = (3 * np.argwhere(left).reshape(-1)[:, None] + np.arange(3)[None, :]).reshape(-1)
+    # surface load on x = Lx: f = sum over face quad points of t N_a nanson (t = (0,0,1))
+    op = ofem.OracleProblem(pts, cells, 3, location_fns=[lambda p: np.isclose(p[0], L[0], atol=1e-5)],
+                            tensor_map=None, surface_maps=[lambda u, x: torch.tensor([0.0, 0.0, 1.0])])
+    f = op.compute_residual(torch.zeros(N)).numpy()
+    th = theta_init(len(cells)).numpy()
+    t0 = time.perf_counter()
+    sc = simp_fast.SimpCantilever(pts, cells, bc_rows, f)
+    t_setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    A = sc.assemble(th)
+    t_asm = time.perf_counter() - t0
+    k = 200
+    t0 = time.perf_counter()
+    sc.pcg(A, sc.f, 1e-30, iters=k)
+    t_pcg = (time.perf_counter() - t0) / k
+    t0 = time.perf_counter()
+    u, _ = sc.pcg(A, sc.f, 1e-30, iters=5)
+    dE = 3.0 * (1 - 1e-3) * th.reshape(-1) ** 2
+    _ = -dE * np.einsum("ci,cij,cj->c", u[sc.dofs], sc.K0, u[sc.dofs])
+    t_vjp = time.perf_counter() - t0 - 5 * t_pcg
+    _, cells_full, nodes_full, nnz_full = workload_name(n)
+    cs = len(cells)
+    nnz_s = A.nnz
+    est = (t_setup + t_asm) * cells_full / cs + t_pcg * nnz_full / nnz_s * (iters_full[0] + iters_full[1]) + \
+        max(t_vjp, 0.0) * cells_full / cs
+    try:
+        from threadpoolctl import threadpool_info
+        blas = max((i.get("num_threads", 1) for i in threadpool_info()), default=1)
+    except Exception:  # noqa: BLE001
+        blas = 1
+    return {"value": est, "unit": UNIT, "cores": int(blas), "kind": "port",
+            "sample": (f"oracle (numpy/scipy FP64) on HEX8 {sample[0]}x{sample[1]}x{sample[2]} ({cs} cells): "
+                       f"element tangents + COO assembly {t_setup + t_asm:.2f}s, {k} Jacobi-PCG iterations "
+                       f"{t_pcg * 1e3:.2f} ms each, VJP; scaled by cells and nnz to the full workload with "
+                       f"{iters_full[0]}+{iters_full[1]} PCG iterations (forward+adjoint); SpMV is scipy's "
+                       f"single-threaded CSR kernel, BLAS threads {blas}"),
+            "host_cores": len(os.sched_getaffinity(0))}
+
+
+def bench_reference(args):
+    n = tuple(args.size)
+    name, cells, nodes, nnz = workload_name(n)
+    iters = FULL_SIZE_PCG_ITERS or _default_iters(n)
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(n, iters)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(n, iters))
+    wall = time.perf_counter() - t0
+    v = statistics.median([x["value"] for x in vals])
+    cb = dict(vals[-1], value=v)
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall / max(args.steps, 1) * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": name, "precision": "fp64", "tolerance": RTOL, "solver": "Jacobi PCG (scipy)"},
+            "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def _default_iters(n):
+    # Jacobi-PCG iterations grow ~linearly with the longest mesh dimension for this cantilever
+    return (int(12 * max(n)), int(12 * max(n)))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, nargs=3, default=list(DEFAULT_SIZE))
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            bench_reference(args)
+        return
+
+    import torch
+    import jax_fem_gb300 as jf
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    n = tuple(args.size)
+    name, cells, nodes, nnz = workload_name(n)
+    prob = make_problem(n)
+    eng = prob._engine
+    theta0 = theta_init(cells).cuda()
+    peak, peak_kind = measured_peak()
+    lib = jf._lib.load()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(precision, steps, warmup, record=None):
+        fwd_opts, adj_opts = options(precision)
+        fwd = jf.ad_wrapper(prob, fwd_opts, adj_opts)
+        for _ in range(warmup):
+            run_steps(prob, fwd, theta0)
+        eng.solve_log.clear()
+        for k in eng.timing:
+            eng.timing[k] = 0.0
+        barrier()
+        s = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = lib.fem_kernel_launches()
+        e0.record(s)
+        out = None
+        for _ in range(steps):
+            out = run_steps(prob, fwd, theta0)
+        e1.record(s)
+        barrier()
+        launches = lib.fem_kernel_launches() - l0
+        t = e0.elapsed_time(e1) / 1e3
+        if dist is not None:
+            tt = torch.tensor([t], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t = tt.item()
+        its = [r["iterations"] for r in eng.solve_log]
+        return t, out, launches, its, dict(eng.timing)
+
+    # ---- mixed (headline) ------------------------------------------------------
+    with ClockSampler(local) as clk:
+        t_mx, (J_mx, g_mx, u_mx), launches, its_mx, phases_mx = timed("mixed", args.steps, args.warmup)
+    clocks = clk.summary()
+    roof = spmv_roofline(prob, peak)
+
+    # ---- plain FP64 ------------------------------------------------------------
+    fp64 = None
+    if not args.no_fp64:
+        t_64, (J_64, g_64, u_64), _, its_64, phases_64 = timed("fp64", max(1, args.steps), max(3, args.warmup))
+        roof.update({k: v for k, v in spmv_roofline(prob, peak).items() if k == "fp64"})
+        rel = lambda a, b: float((a - b).abs().max() / b.abs().max())
+        fp64 = {"value": t_64 / args.steps, "unit": UNIT, "speedup_mixed_vs_fp64": (t_64 / args.steps) / (t_mx / args.steps),
+                "pcg_iterations": its_64, "phases_s": {k: v / args.steps for k, v in phases_64.items()},
+                "errors_mixed_vs_fp64": {"solution": rel(u_mx, u_64), "compliance": abs(J_mx.item() - J_64.item()) / abs(J_64.item()),
+                                         "gradient": rel(g_mx, g_64)}}
+
+    # ---- e2e through the public API with host buffers ----------------------------
+    fwd_opts, adj_opts = options("mixed")
+    fwd = jf.ad_wrapper(prob, fwd_opts, adj_opts)
+    theta_host = theta_init(cells).pin_memory()
+    grad_host = torch.empty_like(theta_host).pin_memory()
+    J_host = torch.empty(1, dtype=torch.float64).pin_memory()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        th = theta_host.to("cuda", non_blocking=True)
+        J, g, _ = run_steps(prob, fwd, th)
+        grad_host.copy_(g, non_blocking=True)
+        J_host.copy_(J.reshape(1), non_blocking=True)
+        torch.cuda.synchronize()
+    barrier()
+    t_e2e = (time.perf_counter() - t0)
+    h2d = theta_host.numel() * 8
+    d2h = grad_host.numel() * 8 + 8
+
+    # ---- CPU baseline (rank 0, N=1) ----------------------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        it_full = (its_64[0], its_64[1]) if fp64 is not None and len(its_64) >= 2 else _default_iters(n)
+        try:
+            cpu = cpu_baseline(n, it_full)
+        except Exception as exc:  # noqa: BLE001
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
+
+    f32 = roof.get("fp32", {})
+    traffic = traffic_from_profile(nnz)
+    value = t_mx / args.steps / world
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_mx / args.steps * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 tangent/Krylov + f64 residuals, dots, refinement",
+        "data": "synthetic",
+        "config": {"workload": name, "precision": "mixed", "tolerance": RTOL,
+                   "solver": "block-Jacobi PCG (FP32) in FP64 Newton refinement; adjoint FP32 PCG in FP64 refinement",
+                   "l2": "inputs larger than L2 (FP32 CSR values alone are 0.98 GB > 129 MB)",
+                   "replicas": "one independent problem per GPU (no data-path collective)"},
+        "pcg_iterations": its_mx,
+        "phases_s": {k: v / args.steps for k, v in phases_mx.items()},
+        "fp64": fp64,
+        "e2e": {"value": t_e2e / args.steps / world, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": f32.get("achieved_gbs"), "peak": peak, "unit": "GB/s",
+                     "frac": f32.get("frac"), "traffic": traffic, "kernel": "spmv_kernel<3,float> (fem_spmv FP32)",
+                     "peak_kind": peak_kind, "algorithmic_bytes": f32.get("algorithmic_bytes"),
+                     "launch_seconds": f32.get("seconds"), "fp64": roof.get("fp64")},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": int(launches),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -93,6 +93,9 @@ typedef struct fem_material_t {
 /* ---- library ------------------------------------------------------------- */
 const char* fem_last_error(void);
 int fem_version(void);
+/* Number of kernels this library has launched in the process (diagnostic counter; no
+ * counterpart in the reference). */
+uint64_t fem_kernel_launches(void);
 /* Element sizes: nodes per cell, volume quad points, faces, face quad points. */
 int fem_element_info(int32_t elem_type, int32_t* nodes_per_cell, int32_t* n_quads,
                      int32_t* n_faces, int32_t* n_face_quads);

@@ -58,6 +58,7 @@ PMESH, PPAT, PMAT = C.POINTER(FemMesh), C.POINTER(FemPattern), C.POINTER(FemMate
 SIGNATURES = {
     "fem_last_error": ([], C.c_char_p),
     "fem_version": ([], C.c_int),
+    "fem_kernel_launches": ([], C.c_uint64),
     "fem_element_info": ([I32, PI32, PI32, PI32, PI32], C.c_int),
     "fem_element_tables": ([I32, PF64, PF64, PF64, PF64, PF64, PF64, PF64, PI32], C.c_int),
     "fem_pattern_workspace": ([I64, I32, I64, PSZ], C.c_int),

@@ -229,6 +229,7 @@ extern "C" int fem_quad_points(const fem_mesh_t* mesh, double* x_out, double* jx
   const int64_t work = mesh->n_cells * tab.nq;
   quad_points_kernel<<<grid_for(work, 256), 256, 0, as_stream(stream)>>>(tab, mesh->coords, mesh->conn,
                                                                          mesh->n_cells, x_out, jxw_out);
+  note_launches(1);
   return check_launch("quad_points_kernel");
 }
 
@@ -243,6 +244,7 @@ extern "C" int fem_face_quad_points(const fem_mesh_t* mesh, const int32_t* face_
   const int64_t work = n_faces * ft.nfq;
   face_points_kernel<<<grid_for(work, 128), 128, 0, as_stream(stream)>>>(ft, mesh->coords, mesh->conn, face_cells,
                                                                          face_ids, n_faces, x_out, nanson_out);
+  note_launches(1);
   return check_launch("face_points_kernel");
 }
 
@@ -255,6 +257,7 @@ extern "C" int fem_body_load(const fem_mesh_t* mesh, const double* f_qp, double*
   const int64_t work = mesh->n_cells * tab.nn;
   body_load_kernel<<<grid_for(work, 256), 256, 0, as_stream(stream)>>>(tab, mesh->vec, mesh->coords, mesh->conn,
                                                                        mesh->n_cells, f_qp, out);
+  note_launches(1);
   return check_launch("body_load_kernel");
 }
 
@@ -269,6 +272,7 @@ extern "C" int fem_surface_load(const fem_mesh_t* mesh, const int32_t* face_cell
   const int64_t work = n_faces * ft.nn;
   surface_load_kernel<<<grid_for(work, 128), 128, 0, as_stream(stream)>>>(
       ft, mesh->vec, mesh->coords, mesh->conn, face_cells, face_ids, n_faces, t_qp, out);
+  note_launches(1);
   return check_launch("surface_load_kernel");
 }
 

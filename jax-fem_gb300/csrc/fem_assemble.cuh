@@ -321,6 +321,7 @@ int launch_cell_kernel(const AsmParams& P, cudaStream_t stream) {
   if (grid > tiles) grid = tiles;
   if (grid < 1) grid = 1;
   kern<<<(unsigned)grid, L::THREADS, smem, stream>>>(P);
+  note_launches(1);
   return check_launch("cell_kernel");
 }
 

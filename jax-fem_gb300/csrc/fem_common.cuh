@@ -14,6 +14,8 @@ namespace fem {
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
 int check_launch(const char* what);
+// Count kernel launches (fem_kernel_launches); call next to each <<<...>>>.
+void note_launches(int n);
 
 #define FEM_REQUIRE(cond, msg)                                   \
   do {                                                           \

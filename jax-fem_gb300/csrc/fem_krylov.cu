@@ -486,6 +486,7 @@ static void launch_spmv(const fem_pattern_t* pat, int64_t n_nodes, const T* vals
   else
     spmv_kernel<VEC, T, 2><<<g, SPMV_THREADS, 0, s>>>(n_nodes, pat->block_ptr, pat->block_cols, vals, x, y, a, C, op,
                                                       partials, 0);
+  note_launches(1);
 }
 
 static int poll(KCtl* C, cudaStream_t s, KCtl* host) {
@@ -506,8 +507,10 @@ static int pcg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, co
   T* q = reinterpret_cast<T*>(w.vecs + 3 * w.vec_bytes);
   KCtl* C = w.ctl;
   init_ctl_kernel<<<1, 32, 0, s>>>(C, rtol * rtol, atol * atol, (long long)maxiter);
+  note_launches(1);
   launch_spmv<VEC, T>(pat, n_nodes, vals, x, q, nullptr, nullptr, FIN_NONE, nullptr, 0, s);
   pcg_init_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, b, q, r, z, p, pc, C, w.partials);
+  note_launches(1);
   int rc = check_launch("pcg init");
   if (rc) return rc;
   KCtl h;
@@ -519,7 +522,9 @@ static int pcg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, co
     for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
       launch_spmv<VEC, T>(pat, n_nodes, vals, p, q, p, C, FIN_PCG_ALPHA, w.partials, 1, s);
       pcg_update_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, x, r, z, p, q, pc, C, w.partials);
+      note_launches(1);
       pcg_direction_kernel<T><<<vec_grid(n), VTHREADS, 0, s>>>(n, p, z, C);
+      note_launches(1);
     }
     rc = check_launch("pcg iteration");
     if (rc) return rc;
@@ -541,8 +546,10 @@ static int bicg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, c
   T *r = v[0], *rhat = v[1], *p = v[2], *phat = v[3], *q = v[4], *sv = v[5], *shat = v[6], *t = v[7];
   KCtl* C = w.ctl;
   init_ctl_kernel<<<1, 32, 0, s>>>(C, tol * tol, atol * atol, (long long)maxiter);
+  note_launches(1);
   launch_spmv<VEC, T>(pat, n_nodes, vals, x, q, nullptr, nullptr, FIN_NONE, nullptr, 0, s);
   bicg_init_kernel<T><<<vec_grid(n), VTHREADS, 0, s>>>(n, b, q, r, rhat, p, C, w.partials);
+  note_launches(1);
   int rc = check_launch("bicgstab init");
   if (rc) return rc;
   KCtl h;
@@ -553,10 +560,13 @@ static int bicg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, c
     if (h.done || launched >= maxiter) break;
     for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
       bicg_p_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, p, q, phat, pc, C);
+      note_launches(1);
       launch_spmv<VEC, T>(pat, n_nodes, vals, phat, q, rhat, C, FIN_BICG_ALPHA, w.partials, 1, s);
       bicg_s_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, q, sv, shat, pc, C, w.partials);
+      note_launches(1);
       launch_spmv<VEC, T>(pat, n_nodes, vals, shat, t, sv, C, FIN_BICG_OMEGA, w.partials, 2, s);
       bicg_update_kernel<T><<<vec_grid(n), VTHREADS, 0, s>>>(n, x, r, rhat, phat, sv, shat, t, C, w.partials);
+      note_launches(1);
     }
     rc = check_launch("bicgstab iteration");
     if (rc) return rc;
@@ -608,6 +618,7 @@ extern "C" int fem_zero_rows(const fem_pattern_t* pat, int32_t vec, int32_t prec
   else
     zero_rows_kernel<double><<<grid_for(n_rows, 128), 128, 0, s>>>(vec, pat->block_ptr, pat->indptr, pat->diag,
                                                                    (double*)vals, rows, n_rows, diag_value);
+  note_launches(1);
   return check_launch("zero_rows");
 }
 
@@ -617,6 +628,7 @@ extern "C" int fem_apply_bc_vec(double* res, const double* dofs, const int32_t* 
   if (n_rows == 0) return FEM_OK;
   FEM_REQUIRE(res && dofs && rows && values, "NULL argument");
   apply_bc_vec_kernel<<<grid_for(n_rows, 256), 256, 0, as_stream(stream)>>>(res, dofs, rows, values, n_rows, scale);
+  note_launches(1);
   return check_launch("apply_bc_vec");
 }
 
@@ -635,6 +647,7 @@ extern "C" int fem_precond_setup(const fem_pattern_t* pat, int64_t n_nodes, int3
     if (vec == 3) precond_setup_kernel<3, double><<<g, 256, 0, s>>>(n_nodes, pat->block_ptr, pat->block_cols, (const double*)vals, pc_kind, (double*)pc);
     else precond_setup_kernel<1, double><<<g, 256, 0, s>>>(n_nodes, pat->block_ptr, pat->block_cols, (const double*)vals, pc_kind, (double*)pc);
   }
+  note_launches(1);
   return check_launch("precond_setup");
 }
 
@@ -723,10 +736,12 @@ extern "C" int fem_dot(int32_t precision, const void* x, const void* y, int64_t 
   cudaStream_t s = as_stream(stream);
   KWs w = carve(ws, 0, FEM_F64);
   init_ctl_kernel<<<1, 32, 0, s>>>(w.ctl, 0.0, 0.0, 0);
+  note_launches(1);
   const int g = vec_grid(n > 0 ? n : 1);
   if (precision == FEM_F32)
     dot_kernel<float><<<g, VTHREADS, 0, s>>>(n, (const float*)x, (const float*)y, w.ctl, w.partials, out);
   else
     dot_kernel<double><<<g, VTHREADS, 0, s>>>(n, (const double*)x, (const double*)y, w.ctl, w.partials, out);
+  note_launches(1);
   return check_launch("dot");
 }

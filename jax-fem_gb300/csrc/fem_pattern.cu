@@ -227,6 +227,7 @@ static void launch_rows(int elem, const int32_t* conn, int npc, int64_t n_nodes,
     node_rows_kernel<256, FILL><<<g, 128, 0, s>>>(conn, npc, n_nodes, w.nc_ptr, w.nc_idx, row_len, bp, bcols, w.err);
   else
     node_rows_kernel<128, FILL><<<g, 128, 0, s>>>(conn, npc, n_nodes, w.nc_ptr, w.nc_idx, row_len, bp, bcols, w.err);
+  note_launches(1);
 }
 
 }  // namespace fem
@@ -252,10 +253,14 @@ extern "C" int fem_pattern_count(int32_t elem_type, const int32_t* conn, int64_t
   FEM_CUDA(cudaMemsetAsync(w.err, 0, sizeof(int), s));
   const int64_t ne = n_cells * npc;
   count_node_cells<<<grid_for(ne, 256), 256, 0, s>>>(conn, ne, n_nodes, w.nc_ptr, w.err);
+  note_launches(1);
   scan_single_block<<<1, SCAN_THREADS, 0, s>>>(w.nc_ptr, n_nodes);
+  note_launches(1);
   fill_node_cells<<<grid_for(ne, 256), 256, 0, s>>>(conn, ne, npc, n_nodes, w.nc_ptr, w.cursor, w.nc_idx);
+  note_launches(1);
   launch_rows<false>(elem_type, conn, npc, n_nodes, w, block_ptr, nullptr, nullptr, s);
   scan_single_block<<<1, SCAN_THREADS, 0, s>>>(block_ptr, n_nodes);
+  note_launches(1);
   int rc = check_launch("pattern count kernels");
   if (rc) return rc;
   rc = read_err(w.err, s, "fem_pattern_count");
@@ -290,6 +295,7 @@ extern "C" int fem_pattern_slots(int32_t elem_type, const int32_t* conn, int64_t
   FEM_CUDA(cudaGetSymbolAddress(reinterpret_cast<void**>(&err), g_pattern_err));
   FEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
   slots_kernel<<<grid_for(n_cells * npc, 256), 256, 0, s>>>(conn, npc, n_cells, block_ptr, block_cols, slots, err);
+  note_launches(1);
   int rc = check_launch("slots kernel");
   if (rc) return rc;
   return read_err(err, s, "fem_pattern_slots");
@@ -305,6 +311,7 @@ extern "C" int fem_pattern_scalar(int64_t n_nodes, int32_t vec, const int64_t* b
   FEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
   scalar_view_kernel<<<grid_for(n_nodes, 256), 256, 0, s>>>(n_nodes, vec, block_ptr, block_cols, indptr, diag, indices,
                                                             err);
+  note_launches(1);
   int rc = check_launch("scalar view kernel");
   if (rc) return rc;
   return read_err(err, s, "fem_pattern_scalar");

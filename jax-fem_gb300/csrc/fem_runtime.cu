@@ -1,4 +1,5 @@
 // Library runtime: error text, device queries, version.
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -8,6 +9,9 @@
 namespace fem {
 
 static thread_local std::string g_last_error;
+static std::atomic<unsigned long long> g_launches{0};
+
+void note_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 
@@ -42,3 +46,5 @@ int sm_count() {
 extern "C" const char* fem_last_error(void) { return fem::g_last_error.c_str(); }
 
 extern "C" int fem_version(void) { return 100; }
+
+extern "C" uint64_t fem_kernel_launches(void) { return (uint64_t)fem::g_launches.load(); }

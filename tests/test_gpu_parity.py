@@ -111,13 +111,17 @@ def test_bicgstab_matches_jax_iteration(cuda):
     Ao = ofem.assemble_petsc(oprob)
     bo = b.cpu().numpy()
     d = Ao.diagonal()
-    # same iterate after a fixed number of steps (before rounding differences grow)
-    for k in (1, 2, 10):
+    # Same iterate after a fixed number of steps.  With the Jacobi preconditioner this
+    # recurrence amplifies rounding ~100x per step (on the CPU alone, v/d versus v*(1/d)
+    # already differs by 3e-5 after 10 steps), so preconditioned iterates are compared
+    # over the first steps and the unpreconditioned iteration over 10 steps.
+    for k, pc, tol in ((1, True, 1e-13), (2, True, 1e-11), (3, True, 1e-8), (10, False, 1e-12)):
         x = torch.zeros_like(b)
-        it, rn, st = eng.krylov("bicgstab", A, b, x, jf._lib.FEM_PC_JACOBI, 1e-10, 1e-10, k)
-        xo, ito = osolve.bicgstab_jax(Ao, bo, None, lambda v: v / d, 1e-10, 1e-10, k)
+        it, rn, st = eng.krylov("bicgstab", A, b, x, jf._lib.FEM_PC_JACOBI if pc else jf._lib.FEM_PC_NONE,
+                                1e-10, 1e-10, k)
+        xo, ito = osolve.bicgstab_jax(Ao, bo, None, (lambda v: v / d) if pc else None, 1e-10, 1e-10, k)
         assert it == ito == k and st == jf._lib.FEM_SOLVE_MAXITER
-        assert np.abs(x.cpu().numpy() - xo).max() <= 1e-9 * np.abs(xo).max()
+        assert np.abs(x.cpu().numpy() - xo).max() <= tol * np.abs(xo).max()
     # full solve: same stopping rule, iteration counts within rounding drift
     x = torch.zeros_like(b)
     it, rn, st = eng.krylov("bicgstab", A, b, x, jf._lib.FEM_PC_JACOBI, 1e-10, 1e-10, 10000)
