@@ -42,7 +42,15 @@ enum {
 
 /* ---- enumerations -------------------------------------------------------- */
 enum { FEM_HEX8 = 1, FEM_TET10 = 2, FEM_TET4 = 3 };          /* jax_fem/basis.py:19-114 */
-enum { FEM_F32 = 0, FEM_F64 = 1 };
+enum {
+  FEM_F32 = 0,
+  FEM_F64 = 1,
+  FEM_DF48 = 2   /* matrix values as FP32 hi + int16 correction q (a = hi + q*ulp(hi)/2^16, a
+                    40-bit mantissa in 6 bytes): hi[nnz] floats, then at byte offset
+                    round_up(4*nnz, 256) q[nnz] int16.  Vectors for FEM_DF48 SpMV: x is the
+                    (hi[n], lo[n]) float pair of fem_vector_split, y is FP64.  Arithmetic is
+                    double-float on FP32 pipes (error-free two-product / two-sum). */
+};
 enum {                                                       /* built-in tensor maps     */
   FEM_MAT_LAPLACE = 1,        /* consts: [k]                      test_linear_poisson.py:15-17 */
   FEM_MAT_LINEAR_ELASTIC = 2, /* consts: [E, nu]                  test_linear_elasticity_cube.py:15-26 */
@@ -150,7 +158,9 @@ int fem_surface_load(const fem_mesh_t* mesh, const int32_t* face_cells, const in
  *          FEM_OUT_APPLY     apply_out += K(u) w            (FP64 always)
  * Outputs are accumulated (the caller zeroes them).  bc_mode controls which
  * matrix entries are skipped (FEM_BC_*); bc_mask is one byte per dof.  With a
- * bc_mask, FEM_OUT_RESIDUAL / FEM_OUT_APPLY skip Dirichlet rows too. */
+ * bc_mask, FEM_OUT_RESIDUAL / FEM_OUT_APPLY skip Dirichlet rows too, and
+ * FEM_OUT_APPLY with FEM_BC_SYMMETRIC also treats w as zero on Dirichlet dofs
+ * (the action of the eliminated operator K_ff). */
 int fem_assemble(const fem_mesh_t* mesh, const fem_material_t* mat, const fem_pattern_t* pat,
                  int32_t outputs, int32_t precision, const double* u, const double* w,
                  const uint8_t* bc_mask, int32_t bc_mode, double* residual, void* vals,
@@ -181,6 +191,12 @@ int fem_apply_bc_vec(double* res, const double* dofs, const int32_t* rows, const
  * and PETSc KSPCG/KSPBCGS with PCJACOBI / PCBJACOBI (solver.py:109-134). */
 int fem_spmv(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
              const void* vals, const void* x, void* y, void* stream);
+/* Bytes of a value buffer of nnz entries in `precision` (FEM_F32 / FEM_F64 / FEM_DF48). */
+int fem_matrix_bytes(int64_t nnz, int32_t precision, size_t* bytes);
+/* FP64 values -> FEM_DF48 buffer (fem_matrix_bytes(nnz, FEM_DF48)). */
+int fem_matrix_split(const double* vals64, int64_t nnz, void* vals_df, void* stream);
+/* FP64 vector -> (hi[n], lo[n]) float pair, the FEM_DF48 SpMV input. */
+int fem_vector_split(const double* x, int64_t n, float* x_df, void* stream);
 /* Jacobi: pc = 1/diag (n_dofs values); block Jacobi: inverse node blocks (n_nodes*vec*vec). */
 int fem_precond_setup(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
                       const void* vals, int32_t pc_kind, void* pc, void* stream);
@@ -197,6 +213,24 @@ int fem_bicgstab(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t
                  const void* vals, int32_t pc_kind, const void* pc, const void* b, void* x,
                  double tol, double atol, int64_t maxiter, void* ws, size_t ws_bytes,
                  int64_t* iterations, double* res_norm, int32_t* status, void* stream);
+
+/* Mixed-precision PCG with FP64 reliable updates.  precision FEM_F32: FP32 matrix, FP32
+ * vectors; FEM_DF48: DF48 matrix (double-float SpMV on FP32 pipes), FP64 vectors and dots.
+ * The preconditioner pc32 is FP32 in both cases.
+ * Solves the Dirichlet-eliminated system K_ff x_f = b_f (x_b = b_b on Dirichlet dofs)
+ * where K is the tangent of `mat` at u_lin.  x (FP64, in/out) holds the initial guess.
+ * When the FP32 recursive residual has fallen by `delta` since the last replacement,
+ * the FP32 increment is added into x in FP64 and the residual is replaced by the true
+ * residual b - K x computed in FP64 by the matrix-free tangent action; the search
+ * direction is kept.  Stops when the FP64 true residual satisfies
+ * ||b - K x||_2 <= max(rtol ||b||_2, atol).  ws >= fem_krylov_workspace(n, FEM_F64).
+ * Replaces the reference's FP64-only linear solve in newton_step / implicit_vjp
+ * (jax_fem/solver.py:390-421, 1399-1409) for the mixed-precision path.  Syncs. */
+int fem_pcg_refined(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision, const void* vals32,
+                    int32_t pc_kind, const void* pc32, const fem_mesh_t* mesh, const fem_material_t* mat,
+                    const double* u_lin, const uint8_t* bc_mask, const double* b, double* x,
+                    double rtol, double atol, double delta, int64_t maxiter, void* ws, size_t ws_bytes,
+                    int64_t* iterations, int64_t* updates, double* res_norm, int32_t* status, void* stream);
 
 /* ---- vector helpers for refinement / Newton ------------------------------ */
 /* dst32[i] = mask[i] ? 0 : (float)src64[i]  (mask may be NULL) */

@@ -121,7 +121,8 @@ cell_kernel(const AsmParams P) {
           sU[k * VEC + v] = P.u ? T(P.u[dof]) : T(0);
           if (need_w) {
             T wv = T(P.w[dof]);
-            if (KMODE == KMODE_VJP && P.bc && P.bc[dof]) wv = T(0);
+            // VJP: multiplier masked on Dirichlet dofs; APPLY with FEM_BC_SYMMETRIC: K_ff w_f
+            if (P.bc && P.bc[dof] && (KMODE == KMODE_VJP || P.bc_mode == FEM_BC_SYMMETRIC)) wv = T(0);
             sW[k * VEC + v] = wv;
           }
         }

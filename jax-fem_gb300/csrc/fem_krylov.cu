@@ -29,13 +29,17 @@ constexpr int CHUNK = 16;
 
 struct KCtl {
   double rho, rho_prev, alpha, beta, omega, thresh2, rr, bb, d0, d1, ss;
+  double rmax2, delta2, rr_true, check2;   // reliable-update PCG
   long long iter, maxiter;
   int done, status, exit_early, pad;
   unsigned int ticket[4];
 };
 
+// internal status: the FP32 iteration paused for an FP64 residual replacement
+constexpr int SOLVE_UPDATE = 10;
+
 enum { FIN_NONE = 0, FIN_PCG_INIT, FIN_PCG_ALPHA, FIN_PCG_UPDATE, FIN_BICG_INIT, FIN_BICG_ALPHA, FIN_BICG_S,
-       FIN_BICG_OMEGA, FIN_BICG_UPDATE, FIN_DOT };
+       FIN_BICG_OMEGA, FIN_BICG_UPDATE, FIN_DOT, FIN_REF_BB, FIN_REF_TRUE, FIN_PCGR_START, FIN_PCGR_UPDATE };
 
 __device__ __forceinline__ bool finite(double v) { return isfinite(v); }
 
@@ -110,6 +114,34 @@ __device__ void finalize(KCtl* C, int op, const double (&d)[3], double* dot_out)
     case FIN_DOT:
       *dot_out = d[0];
       break;
+    case FIN_REF_BB:  // d0 = b.b (FP64): true-residual target and the FP32 pause threshold
+      C->bb = d[0];
+      C->thresh2 = fmax(C->thresh2 * d[0], C->d1);
+      C->check2 = 0.25 * C->thresh2;
+      break;
+    case FIN_REF_TRUE:  // d0 = ||b - A x||^2 in FP64
+      C->rr_true = d[0];
+      break;
+    case FIN_PCGR_START: {  // d = (r.z, r.r) after a residual replacement
+      if (!finite(d[0]) || !finite(d[1])) { C->status = FEM_SOLVE_NAN; C->done = 1; break; }
+      C->beta = (C->iter > 0 && C->rho != 0.0) ? d[0] / C->rho : 0.0;
+      C->rho = d[0];
+      C->rr = d[1];
+      C->rmax2 = d[1];
+      C->done = 0;
+      C->status = FEM_SOLVE_CONVERGED;
+      break;
+    }
+    case FIN_PCGR_UPDATE: {  // d = (r.z, r.r) of the FP32 recursive residual
+      C->iter += 1;
+      C->rr = d[1];
+      if (!finite(d[0]) || !finite(d[1])) { C->status = FEM_SOLVE_NAN; C->done = 1; break; }
+      if (d[1] <= C->check2 || d[1] <= C->delta2 * C->rmax2) { C->status = SOLVE_UPDATE; C->done = 1; break; }
+      if (C->iter >= C->maxiter) { C->status = FEM_SOLVE_MAXITER; C->done = 1; break; }
+      C->beta = d[0] / C->rho;
+      C->rho = d[0];
+      break;
+    }
     default:
       break;
   }
@@ -148,52 +180,179 @@ __device__ __forceinline__ void reduce_and_finalize(double (&v)[3], KCtl* C, int
   }
 }
 
-// ---- SpMV (warp per node row, lane per block column) -------------------------
-// y = A x; optional fused dots d0 = a.y, d1 = y.y and last-CTA finalize op.
-template <int VEC, typename T, int ND>
-__global__ void __launch_bounds__(SPMV_THREADS) spmv_kernel(int64_t n_nodes, const int64_t* __restrict__ bp,
-                                                            const int32_t* __restrict__ bcols,
-                                                            const T* __restrict__ vals, const T* __restrict__ x,
-                                                            T* __restrict__ y, const T* __restrict__ a, KCtl* C,
-                                                            int op, double* partials, int ticket_id) {
+// ---- SpMV -------------------------------------------------------------------------
+// Eight lanes per node row (vec scalar rows), four node rows per warp: lane `sub` takes
+// block columns k = sub, sub+8, ..., loads the block column index and the vec x-entries
+// once per block and all vec*vec values of the block, and the eight partial sums of each
+// scalar row meet in three xor-shuffle steps.  Value formats:
+//   FMT_F32   float values, float x, float y
+//   FMT_F64   double values, double x, double y
+//   FMT_DF    "double-float" values: float hi plus an int16 correction q scaled to
+//             the ulp of hi (a = hi + q * ulp(hi) / 2^16, a 40-bit mantissa in 6 bytes),
+//             x given as a (hi, lo) float pair, arithmetic in error-free FP32
+//             transformations (two-product / two-sum), y written in FP64.  This keeps
+//             the FP64-level accuracy of the operator while using only FP32 pipes.
+enum { FMT_F32 = 0, FMT_F64 = 1, FMT_DF = 2 };
+constexpr int SPMV_G = 8;
+
+__device__ __forceinline__ float df_lo_scale(float hi) {
+  const int e = (__float_as_int(hi) >> 23) & 0xFF;
+  return e > 39 ? __int_as_float((e - 39) << 23) : 0.0f;   // 2^(e - 166) = ulp(hi) / 2^16
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& err) {
+  s = a + b;
+  const float bb = s - a;
+  err = (a - (s - bb)) + (b - bb);
+}
+
+template <int FMT>
+struct SpmvTypes;
+template <> struct SpmvTypes<FMT_F32> { using V = float; using X = float; using Y = float; };
+template <> struct SpmvTypes<FMT_F64> { using V = double; using X = double; using Y = double; };
+template <> struct SpmvTypes<FMT_DF> { using V = float; using X = float; using Y = double; };
+
+template <int VEC, int FMT, int ND>
+__global__ void __launch_bounds__(SPMV_THREADS)
+spmv_kernel(int64_t n_nodes, const int64_t* __restrict__ bp, const int32_t* __restrict__ bcols,
+            const typename SpmvTypes<FMT>::V* __restrict__ vals, const int16_t* __restrict__ vlo,
+            const typename SpmvTypes<FMT>::X* __restrict__ x, const float* __restrict__ xlo,
+            typename SpmvTypes<FMT>::Y* __restrict__ y, const typename SpmvTypes<FMT>::Y* __restrict__ a, KCtl* C,
+            int op, double* partials, int ticket_id) {
+  using V = typename SpmvTypes<FMT>::V;
+  using X = typename SpmvTypes<FMT>::X;
   if (C && C->done) return;
   const int lane = threadIdx.x & 31;
-  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int sub = lane & (SPMV_G - 1);
+  // groups of SPMV_G lanes own one node row (VEC scalar rows); lane `sub` takes the
+  // block columns k = sub, sub + G, ... and all VEC x VEC values of each block
+  const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / SPMV_G;
+  const int64_t first = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / SPMV_G;
+  const int64_t warp_first = first - (lane / SPMV_G);
   double dv[3] = {0.0, 0.0, 0.0};
-  for (int64_t i = warp; i < n_nodes; i += nwarps) {
-    const int64_t b0 = bp[i];
-    const int nb = (int)(bp[i + 1] - b0);
-    const T* vrow = vals + (int64_t)VEC * VEC * b0;
-    T acc[VEC];
+  for (int64_t base = warp_first; base < n_nodes; base += groups) {
+    const int64_t i = base + lane / SPMV_G;
+    const bool valid = i < n_nodes;
+    const int64_t b0 = valid ? bp[i] : 0;
+    const int nb = valid ? (int)(bp[i + 1] - b0) : 0;
+    const int64_t rs0 = (int64_t)VEC * VEC * b0;     // first value of scalar row 0
+    const int rstride = VEC * nb;                     // values per scalar row
+    if constexpr (FMT == FMT_DF) {
+      float sh[VEC], sl[VEC];
 #pragma unroll
-    for (int r = 0; r < VEC; ++r) acc[r] = T(0);
-    for (int k = lane; k < nb; k += 32) {
-      const int64_t col = bcols[b0 + k];
-      T xv[VEC];
+      for (int r = 0; r < VEC; ++r) { sh[r] = 0.0f; sl[r] = 0.0f; }
+      for (int k = sub; k < nb; k += SPMV_G) {
+        const int64_t col = (int64_t)VEC * __ldg(bcols + b0 + k);
+        float xh[VEC], xl[VEC];
 #pragma unroll
-      for (int d = 0; d < VEC; ++d) xv[d] = __ldg(x + VEC * col + d);
+        for (int d = 0; d < VEC; ++d) { xh[d] = __ldg(x + col + d); xl[d] = __ldg(xlo + col + d); }
+#pragma unroll
+        for (int r = 0; r < VEC; ++r) {
+          const int64_t o = rs0 + (int64_t)r * rstride + VEC * k;
+#pragma unroll
+          for (int d = 0; d < VEC; ++d) {
+            const float ah = __ldcs(vals + o + d);
+            // ulp(ah) / 2^16 from the exponent bits; q = 0 wherever this would not be a normal float
+            const float sc = __int_as_float((__float_as_int(ah) & 0x7f800000) - (39 << 23));
+            const float al = (float)__ldcs(vlo + o + d) * sc;
+            const float p = ah * xh[d];
+            float err = fmaf(ah, xh[d], -p);
+            err = fmaf(ah, xl[d], err);
+            err = fmaf(al, xh[d], err);
+            float t, te;
+            two_sum(sh[r], p, t, te);
+            sl[r] += te + err;
+            sh[r] = t;
+          }
+        }
+      }
 #pragma unroll
       for (int r = 0; r < VEC; ++r) {
-        const T* vr = vrow + (int64_t)r * VEC * nb + VEC * k;
 #pragma unroll
-        for (int d = 0; d < VEC; ++d) acc[r] += __ldcs(vr + d) * xv[d];
+        for (int o = SPMV_G / 2; o > 0; o >>= 1) {
+          const float oh = __shfl_xor_sync(0xffffffffu, sh[r], o);
+          const float ol = __shfl_xor_sync(0xffffffffu, sl[r], o);
+          float t, te;
+          two_sum(sh[r], oh, t, te);
+          sl[r] += ol + te;
+          sh[r] = t;
+        }
       }
-    }
+      if (valid && sub < VEC) {
+        float h = sh[0], l = sl[0];
 #pragma unroll
-    for (int r = 0; r < VEC; ++r) acc[r] = warp_sum(acc[r]);
-    if (lane < VEC) {
-      T out = acc[0];
+        for (int r = 1; r < VEC; ++r)
+          if (sub == r) { h = sh[r]; l = sl[r]; }
+        const double out = (double)h + (double)l;
+        const int64_t row = (int64_t)VEC * i + sub;
+        y[row] = out;
+        if constexpr (ND >= 1) dv[0] += a[row] * out;
+        if constexpr (ND >= 2) dv[1] += out * out;
+      }
+    } else {
+      V acc[VEC];
 #pragma unroll
-      for (int r = 1; r < VEC; ++r)
-        if (lane == r) out = acc[r];
-      const int64_t row = (int64_t)VEC * i + lane;
-      y[row] = out;
-      if constexpr (ND >= 1) dv[0] += double(a[row]) * double(out);
-      if constexpr (ND >= 2) dv[1] += double(out) * double(out);
+      for (int r = 0; r < VEC; ++r) acc[r] = V(0);
+      for (int k = sub; k < nb; k += SPMV_G) {
+        const int64_t col = (int64_t)VEC * __ldg(bcols + b0 + k);
+        X xv[VEC];
+#pragma unroll
+        for (int d = 0; d < VEC; ++d) xv[d] = __ldg(x + col + d);
+#pragma unroll
+        for (int r = 0; r < VEC; ++r) {
+          const int64_t o = rs0 + (int64_t)r * rstride + VEC * k;
+#pragma unroll
+          for (int d = 0; d < VEC; ++d) acc[r] += __ldcs(vals + o + d) * xv[d];
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < VEC; ++r) {
+#pragma unroll
+        for (int o = SPMV_G / 2; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+      }
+      if (valid && sub < VEC) {
+        V out = acc[0];
+#pragma unroll
+        for (int r = 1; r < VEC; ++r)
+          if (sub == r) out = acc[r];
+        const int64_t row = (int64_t)VEC * i + sub;
+        y[row] = out;
+        if constexpr (ND >= 1) dv[0] += double(a[row]) * double(out);
+        if constexpr (ND >= 2) dv[1] += double(out) * double(out);
+      }
     }
   }
   if constexpr (ND > 0) reduce_and_finalize<ND>(dv, C, op, partials, C->ticket + ticket_id, nullptr);
+}
+
+// DF48 split of an FP64 matrix: hi = fl32(a), q = round((a - hi) * 2^16 / ulp(hi)).
+__global__ void split_df_kernel(const double* __restrict__ v, int64_t n, float* __restrict__ hi,
+                                int16_t* __restrict__ lo) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const double a = v[k];
+    const float h = __double2float_rn(a);
+    const int e = (__float_as_int(h) >> 23) & 0xFF;
+    int q = 0;
+    if (e > 39 && e < 255) {
+      const double rem = a - (double)h;
+      double t = rint(scalbn(rem, 166 - e));
+      t = fmin(fmax(t, -32767.0), 32767.0);
+      q = (int)t;
+    }
+    hi[k] = h;
+    lo[k] = (int16_t)q;
+  }
+}
+
+// (hi, lo) float split of an FP64 vector, the SpMV input of the DF format
+__global__ void split_vec_kernel(const double* __restrict__ v, int64_t n, float* __restrict__ hi,
+                                 float* __restrict__ lo) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const double a = v[k];
+    const float h = __double2float_rn(a);
+    hi[k] = h;
+    lo[k] = __double2float_rn(a - (double)h);
+  }
 }
 
 // ---- vector kernels (thread per node) ----------------------------------------
@@ -249,7 +408,7 @@ __global__ void pcg_init_kernel(int64_t n_nodes, const T* b, const T* q, T* r, T
 // x += alpha p ; r -= alpha q ; z = M r ; dots (r.z, r.r)
 template <int VEC, typename T, int PC>
 __global__ void pcg_update_kernel(int64_t n_nodes, T* x, T* r, T* z, const T* p, const T* q, const T* pc, KCtl* C,
-                                  double* partials) {
+                                  double* partials, int op) {
   if (C->done) return;
   const T alpha = T(C->alpha);
   double dv[3] = {0, 0, 0};
@@ -270,7 +429,137 @@ __global__ void pcg_update_kernel(int64_t n_nodes, T* x, T* r, T* z, const T* p,
       dv[1] += double(rv[c]) * double(rv[c]);
     }
   }
-  reduce_and_finalize<2>(dv, C, FIN_PCG_UPDATE, partials, C->ticket + 1, nullptr);
+  reduce_and_finalize<2>(dv, C, op, partials, C->ticket + 1, nullptr);
+}
+
+// Reliable-update PCG: FP64 true residual r64 = b - A x (A x in ax; Dirichlet rows b - x),
+// its FP32 copy r32, and ||r64||^2.
+__global__ void refine_residual_kernel(int64_t n, const double* b, const double* x, const double* ax,
+                                       const uint8_t* bc, float* r32, KCtl* C, double* partials) {
+  double dv[3] = {0, 0, 0};
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const double r = (bc && bc[k]) ? (b[k] - x[k]) : (b[k] - ax[k]);
+    r32[k] = (float)r;
+    dv[0] += r * r;
+  }
+  reduce_and_finalize<1>(dv, C, FIN_REF_TRUE, partials, C->ticket + 1, nullptr);
+}
+
+// After a residual replacement: z = M r, dots (r.z, r.r); x32 := 0; p := z on the first start.
+template <int VEC, int PC>
+__global__ void pcgr_start_kernel(int64_t n_nodes, const float* r, float* z, float* p, float* x32, const float* pc,
+                                  int first, KCtl* C, double* partials) {
+  double dv[3] = {0, 0, 0};
+  GRID_STRIDE_NODES(i, n_nodes) {
+    float rv[VEC], zv[VEC];
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) rv[c] = r[VEC * i + c];
+    precond<VEC, float, PC>(pc, i, rv, zv);
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) {
+      const int64_t k = VEC * i + c;
+      z[k] = zv[c];
+      x32[k] = 0.0f;
+      if (first) p[k] = zv[c];
+      dv[0] += double(rv[c]) * double(zv[c]);
+      dv[1] += double(rv[c]) * double(rv[c]);
+    }
+  }
+  reduce_and_finalize<2>(dv, C, FIN_PCGR_START, partials, C->ticket + 1, nullptr);
+}
+
+__global__ void accumulate_kernel(double* x64, const float* x32, int64_t n) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    x64[k] += (double)x32[k];
+}
+
+// ---- double-float (DF48) PCG: FP64 vectors, DF48 SpMV, FP32 preconditioner --------
+template <int VEC, int PC>
+__device__ __forceinline__ void precond32(const float* pc, int64_t i, const double (&r)[VEC], double (&z)[VEC]) {
+  float rf[VEC], zf[VEC];
+#pragma unroll
+  for (int c = 0; c < VEC; ++c) rf[c] = (float)r[c];
+  precond<VEC, float, PC>(pc, i, rf, zf);
+#pragma unroll
+  for (int c = 0; c < VEC; ++c) z[c] = (double)zf[c];
+}
+
+__device__ __forceinline__ void split_store(double v, float* hi, float* lo, int64_t k) {
+  const float h = __double2float_rn(v);
+  hi[k] = h;
+  lo[k] = __double2float_rn(v - (double)h);
+}
+
+// z = M r; on the first start p = z (and its (hi, lo) split); dots (r.z, r.r)
+template <int VEC, int PC>
+__global__ void pcgd_start_kernel(int64_t n_nodes, const double* r, double* z, double* p, float* phi, float* plo,
+                                  const float* pc, int first, KCtl* C, double* partials) {
+  double dv[3] = {0, 0, 0};
+  GRID_STRIDE_NODES(i, n_nodes) {
+    double rv[VEC], zv[VEC];
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) rv[c] = r[VEC * i + c];
+    precond32<VEC, PC>(pc, i, rv, zv);
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) {
+      const int64_t k = VEC * i + c;
+      z[k] = zv[c];
+      if (first) { p[k] = zv[c]; split_store(zv[c], phi, plo, k); }
+      dv[0] += rv[c] * zv[c];
+      dv[1] += rv[c] * rv[c];
+    }
+  }
+  reduce_and_finalize<2>(dv, C, FIN_PCGR_START, partials, C->ticket + 1, nullptr);
+}
+
+// x += alpha p ; r -= alpha q ; z = M r ; dots (r.z, r.r)
+template <int VEC, int PC>
+__global__ void pcgd_update_kernel(int64_t n_nodes, double* x, double* r, double* z, const double* p, const double* q,
+                                   const float* pc, KCtl* C, double* partials, int op) {
+  if (C->done) return;
+  const double alpha = C->alpha;
+  double dv[3] = {0, 0, 0};
+  GRID_STRIDE_NODES(i, n_nodes) {
+    double rv[VEC], zv[VEC];
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) {
+      const int64_t k = VEC * i + c;
+      x[k] += alpha * p[k];
+      rv[c] = r[k] - alpha * q[k];
+      r[k] = rv[c];
+    }
+    precond32<VEC, PC>(pc, i, rv, zv);
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) {
+      z[VEC * i + c] = zv[c];
+      dv[0] += rv[c] * zv[c];
+      dv[1] += rv[c] * rv[c];
+    }
+  }
+  reduce_and_finalize<2>(dv, C, op, partials, C->ticket + 1, nullptr);
+}
+
+// p = z + beta p and its (hi, lo) split for the DF48 SpMV
+__global__ void pcgd_direction_kernel(int64_t n, double* p, const double* z, float* phi, float* plo, const KCtl* C) {
+  if (C->done) return;
+  const double beta = C->beta;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const double v = z[k] + beta * p[k];
+    p[k] = v;
+    split_store(v, phi, plo, k);
+  }
+}
+
+// FP64 true residual r = b - A x (Dirichlet rows: b - x) and ||r||^2
+__global__ void refine_residual64_kernel(int64_t n, const double* b, const double* x, const double* ax,
+                                         const uint8_t* bc, double* r, KCtl* C, double* partials) {
+  double dv[3] = {0, 0, 0};
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const double v = (bc && bc[k]) ? (b[k] - x[k]) : (b[k] - ax[k]);
+    r[k] = v;
+    dv[0] += v * v;
+  }
+  reduce_and_finalize<1>(dv, C, FIN_REF_TRUE, partials, C->ticket + 1, nullptr);
 }
 
 template <typename T>
@@ -363,11 +652,12 @@ __global__ void bicg_update_kernel(int64_t n, T* x, T* r, const T* rhat, const T
 }
 
 template <typename T>
-__global__ void dot_kernel(int64_t n, const T* x, const T* y, KCtl* C, double* partials, double* out) {
+__global__ void dot_kernel(int64_t n, const T* x, const T* y, KCtl* C, double* partials, double* out,
+                           int op = FIN_DOT) {
   double dv[3] = {0, 0, 0};
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
     dv[0] += double(x[k]) * double(y[k]);
-  reduce_and_finalize<1>(dv, C, FIN_DOT, partials, C->ticket + 2, out);
+  reduce_and_finalize<1>(dv, C, op, partials, C->ticket + 2, out);
 }
 
 __global__ void init_ctl_kernel(KCtl* C, double thresh2_rel, double atol2, long long maxiter) {
@@ -468,25 +758,48 @@ static int vec_grid(int64_t n) {
   return g > MAX_PARTIAL_BLOCKS ? MAX_PARTIAL_BLOCKS : g;
 }
 
-static int spmv_grid(int64_t n_nodes) {
-  int g = grid_for(n_nodes * 32, SPMV_THREADS, 8);
-  return g > MAX_PARTIAL_BLOCKS ? MAX_PARTIAL_BLOCKS : g;
+
+template <typename K>
+static int spmv_blocks_per_sm(K kern) {
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, SPMV_THREADS, 0) != cudaSuccess || b < 1) b = 4;
+  return b;
+}
+
+// Grid = resident CTAs (no partial waves), capped by the rows to process.
+template <int VEC, int FMT, int ND>
+static void launch_spmv_fmt(const fem_pattern_t* pat, int64_t n_nodes, const void* vals, const int16_t* vlo,
+                            const void* x, const float* xlo, void* y, const void* a, KCtl* C, int op,
+                            double* partials, cudaStream_t s) {
+  using Tp = SpmvTypes<FMT>;
+  auto kern = spmv_kernel<VEC, FMT, ND>;
+  static int per_sm = 0;
+  if (per_sm == 0) per_sm = spmv_blocks_per_sm(kern);
+  const int64_t need = (n_nodes * SPMV_G + SPMV_THREADS - 1) / SPMV_THREADS;
+  int64_t g = (int64_t)sm_count() * per_sm;
+  if (g > need) g = need;
+  if (g > MAX_PARTIAL_BLOCKS) g = MAX_PARTIAL_BLOCKS;
+  if (g < 1) g = 1;
+  kern<<<(unsigned)g, SPMV_THREADS, 0, s>>>(n_nodes, pat->block_ptr, pat->block_cols,
+                                             (const typename Tp::V*)vals, vlo, (const typename Tp::X*)x, xlo,
+                                             (typename Tp::Y*)y, (const typename Tp::Y*)a, C, op, partials, 0);
+  note_launches(1);
+}
+
+template <int VEC, int FMT>
+static void launch_spmv_nd(const fem_pattern_t* pat, int64_t n_nodes, const void* vals, const int16_t* vlo,
+                           const void* x, const float* xlo, void* y, const void* a, KCtl* C, int op,
+                           double* partials, int nd, cudaStream_t s) {
+  if (nd == 0) launch_spmv_fmt<VEC, FMT, 0>(pat, n_nodes, vals, vlo, x, xlo, y, a, C, op, partials, s);
+  else if (nd == 1) launch_spmv_fmt<VEC, FMT, 1>(pat, n_nodes, vals, vlo, x, xlo, y, a, C, op, partials, s);
+  else launch_spmv_fmt<VEC, FMT, 2>(pat, n_nodes, vals, vlo, x, xlo, y, a, C, op, partials, s);
 }
 
 template <int VEC, typename T>
 static void launch_spmv(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, const T* x, T* y, const T* a,
                         KCtl* C, int op, double* partials, int nd, cudaStream_t s) {
-  const int g = spmv_grid(n_nodes);
-  if (nd == 0)
-    spmv_kernel<VEC, T, 0><<<g, SPMV_THREADS, 0, s>>>(n_nodes, pat->block_ptr, pat->block_cols, vals, x, y, a, C, op,
-                                                      partials, 0);
-  else if (nd == 1)
-    spmv_kernel<VEC, T, 1><<<g, SPMV_THREADS, 0, s>>>(n_nodes, pat->block_ptr, pat->block_cols, vals, x, y, a, C, op,
-                                                      partials, 0);
-  else
-    spmv_kernel<VEC, T, 2><<<g, SPMV_THREADS, 0, s>>>(n_nodes, pat->block_ptr, pat->block_cols, vals, x, y, a, C, op,
-                                                      partials, 0);
-  note_launches(1);
+  constexpr int FMT = sizeof(T) == 4 ? FMT_F32 : FMT_F64;
+  launch_spmv_nd<VEC, FMT>(pat, n_nodes, vals, nullptr, x, nullptr, y, a, C, op, partials, nd, s);
 }
 
 static int poll(KCtl* C, cudaStream_t s, KCtl* host) {
@@ -521,7 +834,8 @@ static int pcg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, co
     if (h.done || launched >= maxiter) break;
     for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
       launch_spmv<VEC, T>(pat, n_nodes, vals, p, q, p, C, FIN_PCG_ALPHA, w.partials, 1, s);
-      pcg_update_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, x, r, z, p, q, pc, C, w.partials);
+      pcg_update_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, x, r, z, p, q, pc, C, w.partials,
+                                                                            FIN_PCG_UPDATE);
       note_launches(1);
       pcg_direction_kernel<T><<<vec_grid(n), VTHREADS, 0, s>>>(n, p, z, C);
       note_launches(1);
@@ -577,6 +891,207 @@ static int bicg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, c
   return FEM_OK;
 }
 
+// FP32 PCG with FP64 reliable updates (residual replacement).  The iteration runs on
+// the FP32 matrix; whenever the FP32 recursive residual has fallen by `delta` since the
+// last replacement (or below a quarter of the target), the device pauses, the host adds
+// the FP32 increment into the FP64 solution and recomputes the true residual b - A x in
+// FP64 with the matrix-free tangent action (fem_assemble FEM_OUT_APPLY), which replaces
+// the FP32 residual.  The search direction is kept, so the Krylov recurrence continues
+// instead of restarting.  Convergence is declared only on the FP64 true residual.
+template <int VEC, int PC>
+static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const float* vals, const float* pc,
+                            const fem_mesh_t* mesh, const fem_material_t* mat, const double* u_lin,
+                            const uint8_t* bc, const double* b, double* x, double rtol, double atol, double delta,
+                            int64_t maxiter, void* ws, int64_t* iters, int64_t* updates, double* rnorm,
+                            int32_t* status, cudaStream_t s) {
+  const int64_t n = n_nodes * VEC;
+  KWs w = carve(ws, n, FEM_F64);
+  const size_t f4 = al(sizeof(float) * (size_t)n);
+  float* r = reinterpret_cast<float*>(w.vecs);
+  float* z = reinterpret_cast<float*>(w.vecs + f4);
+  float* p = reinterpret_cast<float*>(w.vecs + 2 * f4);
+  float* q = reinterpret_cast<float*>(w.vecs + 3 * f4);
+  float* x32 = reinterpret_cast<float*>(w.vecs + 4 * f4);
+  double* ax = reinterpret_cast<double*>(w.vecs + 5 * f4);
+  KCtl* C = w.ctl;
+  init_ctl_kernel<<<1, 32, 0, s>>>(C, rtol * rtol, atol * atol, (long long)maxiter);
+  dot_kernel<double><<<vec_grid(n), VTHREADS, 0, s>>>(n, b, b, C, w.partials, nullptr, FIN_REF_BB);
+  note_launches(2);
+  int rc = check_launch("pcg_refined init");
+  if (rc) return rc;
+  auto true_residual = [&]() -> int {
+    FEM_CUDA(cudaMemsetAsync(ax, 0, sizeof(double) * (size_t)n, s));
+    const int r2 = fem_assemble(mesh, mat, pat, FEM_OUT_APPLY, FEM_F64, u_lin, x, bc, FEM_BC_SYMMETRIC, nullptr,
+                                nullptr, ax, s);
+    if (r2) return r2;
+    refine_residual_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(n, b, x, ax, bc, r, C, w.partials);
+    note_launches(1);
+    return check_launch("refine_residual");
+  };
+  rc = true_residual();
+  if (rc) return rc;
+  KCtl h;
+  rc = poll(C, s, &h);
+  if (rc) return rc;
+  int64_t n_updates = 0;
+  int final_status = FEM_SOLVE_CONVERGED;
+  const double delta2 = delta * delta;
+  if (!(h.rr_true <= h.thresh2)) {
+    // first start: z = M r, p = z
+    FEM_CUDA(cudaMemcpyAsync(&C->delta2, &delta2, sizeof(double), cudaMemcpyHostToDevice, s));
+    pcgr_start_kernel<VEC, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, z, p, x32, pc, 1, C, w.partials);
+    note_launches(1);
+    int64_t launched = 0;
+    while (true) {
+      rc = poll(C, s, &h);
+      if (rc) return rc;
+      if (h.done) {
+        if (h.status == SOLVE_UPDATE) {
+          // residual replacement: x += x32 in FP64, r = b - A x in FP64
+          accumulate_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(x, x32, n);
+          note_launches(1);
+          rc = true_residual();
+          if (rc) return rc;
+          rc = poll(C, s, &h);
+          if (rc) return rc;
+          ++n_updates;
+          if (h.rr_true <= h.thresh2) { final_status = FEM_SOLVE_CONVERGED; break; }
+          if (!std::isfinite(h.rr_true)) { final_status = FEM_SOLVE_NAN; break; }
+          if (h.iter >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
+          pcgr_start_kernel<VEC, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, z, p, x32, pc, 0, C,
+                                                                           w.partials);
+          pcg_direction_kernel<float><<<vec_grid(n), VTHREADS, 0, s>>>(n, p, z, C);
+          note_launches(2);
+          continue;
+        }
+        if (h.status == FEM_SOLVE_MAXITER) {
+          accumulate_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(x, x32, n);
+          note_launches(1);
+          rc = true_residual();
+          if (rc) return rc;
+          rc = poll(C, s, &h);
+          if (rc) return rc;
+          final_status = h.rr_true <= h.thresh2 ? FEM_SOLVE_CONVERGED : FEM_SOLVE_MAXITER;
+          break;
+        }
+        final_status = h.status;  // NaN or breakdown
+        break;
+      }
+      if (launched >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
+      for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
+        launch_spmv<VEC, float>(pat, n_nodes, vals, p, q, p, C, FIN_PCG_ALPHA, w.partials, 1, s);
+        pcg_update_kernel<VEC, float, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, x32, r, z, p, q, pc, C,
+                                                                                w.partials, FIN_PCGR_UPDATE);
+        pcg_direction_kernel<float><<<vec_grid(n), VTHREADS, 0, s>>>(n, p, z, C);
+        note_launches(2);
+      }
+      rc = check_launch("pcg_refined iteration");
+      if (rc) return rc;
+    }
+  }
+  if (iters) *iters = h.iter;
+  if (updates) *updates = n_updates;
+  if (rnorm) *rnorm = std::sqrt(h.rr_true);
+  if (status) *status = final_status;
+  return FEM_OK;
+}
+
+// Byte offset of the int16 corrections inside a DF48 value buffer.
+static inline size_t df_lo_offset(int64_t nnz) { return al(sizeof(float) * (size_t)nnz); }
+
+// DF48 PCG with FP64 reliable updates: FP64 CG vectors and dots, the matrix stream in the
+// 6-byte double-float format (SpMV on FP32 pipes, FP64-level accuracy), FP32 block-Jacobi.
+// The FP64 true residual (matrix-free tangent action) replaces the recursive residual
+// whenever it has fallen by `delta`, and is the only convergence test.
+template <int VEC, int PC>
+static int pcg_df_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* vals, const float* pc,
+                       const fem_mesh_t* mesh, const fem_material_t* mat, const double* u_lin, const uint8_t* bc,
+                       const double* b, double* x, double rtol, double atol, double delta, int64_t maxiter, void* ws,
+                       int64_t* iters, int64_t* updates, double* rnorm, int32_t* status, cudaStream_t s) {
+  const int64_t n = n_nodes * VEC;
+  const int64_t nnz = pat->nnzb * VEC * VEC;
+  const float* vhi = static_cast<const float*>(vals);
+  const int16_t* vlo = reinterpret_cast<const int16_t*>(static_cast<const char*>(vals) + df_lo_offset(nnz));
+  KWs w = carve(ws, n, FEM_F64);
+  const size_t d8 = al(sizeof(double) * (size_t)n), f4 = al(sizeof(float) * (size_t)n);
+  double* r = reinterpret_cast<double*>(w.vecs);
+  double* z = reinterpret_cast<double*>(w.vecs + d8);
+  double* p = reinterpret_cast<double*>(w.vecs + 2 * d8);
+  double* q = reinterpret_cast<double*>(w.vecs + 3 * d8);
+  double* ax = reinterpret_cast<double*>(w.vecs + 4 * d8);
+  float* phi = reinterpret_cast<float*>(w.vecs + 5 * d8);
+  float* plo = reinterpret_cast<float*>(w.vecs + 5 * d8 + f4);
+  KCtl* C = w.ctl;
+  init_ctl_kernel<<<1, 32, 0, s>>>(C, rtol * rtol, atol * atol, (long long)maxiter);
+  dot_kernel<double><<<vec_grid(n), VTHREADS, 0, s>>>(n, b, b, C, w.partials, nullptr, FIN_REF_BB);
+  note_launches(2);
+  int rc = check_launch("pcg_df init");
+  if (rc) return rc;
+  auto true_residual = [&]() -> int {
+    FEM_CUDA(cudaMemsetAsync(ax, 0, sizeof(double) * (size_t)n, s));
+    const int r2 = fem_assemble(mesh, mat, pat, FEM_OUT_APPLY, FEM_F64, u_lin, x, bc, FEM_BC_SYMMETRIC, nullptr,
+                                nullptr, ax, s);
+    if (r2) return r2;
+    refine_residual64_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(n, b, x, ax, bc, r, C, w.partials);
+    note_launches(1);
+    return check_launch("refine_residual64");
+  };
+  rc = true_residual();
+  if (rc) return rc;
+  KCtl h;
+  rc = poll(C, s, &h);
+  if (rc) return rc;
+  int64_t n_updates = 0;
+  int final_status = FEM_SOLVE_CONVERGED;
+  const double delta2 = delta * delta;
+  if (!(h.rr_true <= h.thresh2)) {
+    FEM_CUDA(cudaMemcpyAsync(&C->delta2, &delta2, sizeof(double), cudaMemcpyHostToDevice, s));
+    pcgd_start_kernel<VEC, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, z, p, phi, plo, pc, 1, C,
+                                                                     w.partials);
+    note_launches(1);
+    int64_t launched = 0;
+    while (true) {
+      rc = poll(C, s, &h);
+      if (rc) return rc;
+      if (h.done) {
+        if (h.status == SOLVE_UPDATE || h.status == FEM_SOLVE_MAXITER) {
+          const bool at_max = h.status == FEM_SOLVE_MAXITER;
+          rc = true_residual();
+          if (rc) return rc;
+          rc = poll(C, s, &h);
+          if (rc) return rc;
+          ++n_updates;
+          if (h.rr_true <= h.thresh2) { final_status = FEM_SOLVE_CONVERGED; break; }
+          if (!std::isfinite(h.rr_true)) { final_status = FEM_SOLVE_NAN; break; }
+          if (at_max || h.iter >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
+          pcgd_start_kernel<VEC, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, z, p, phi, plo, pc, 0, C,
+                                                                           w.partials);
+          pcgd_direction_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(n, p, z, phi, plo, C);
+          note_launches(2);
+          continue;
+        }
+        final_status = h.status;  // NaN or breakdown
+        break;
+      }
+      if (launched >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
+      for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
+        launch_spmv_nd<VEC, FMT_DF>(pat, n_nodes, vhi, vlo, phi, plo, q, p, C, FIN_PCG_ALPHA, w.partials, 1, s);
+        pcgd_update_kernel<VEC, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, x, r, z, p, q, pc, C, w.partials,
+                                                                          FIN_PCGR_UPDATE);
+        pcgd_direction_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(n, p, z, phi, plo, C);
+        note_launches(2);
+      }
+      rc = check_launch("pcg_df iteration");
+      if (rc) return rc;
+    }
+  }
+  if (iters) *iters = h.iter;
+  if (updates) *updates = n_updates;
+  if (rnorm) *rnorm = std::sqrt(h.rr_true);
+  if (status) *status = final_status;
+  return FEM_OK;
+}
+
 }  // namespace fem
 
 using namespace fem;
@@ -591,10 +1106,20 @@ static int check_pat(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int
 
 extern "C" int fem_spmv(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision, const void* vals,
                         const void* x, void* y, void* stream) {
-  int rc = check_pat(pat, n_nodes, vec, precision);
+  int rc = check_pat(pat, n_nodes, vec, precision == FEM_DF48 ? FEM_F64 : precision);
   if (rc) return rc;
   FEM_REQUIRE(vals && x && y, "NULL vector");
   cudaStream_t s = as_stream(stream);
+  if (precision == FEM_DF48) {
+    const int64_t n = n_nodes * vec, nnz = pat->nnzb * vec * vec;
+    const float* hi = (const float*)vals;
+    const int16_t* lo = reinterpret_cast<const int16_t*>((const char*)vals + df_lo_offset(nnz));
+    const float* xh = (const float*)x;
+    const float* xl = xh + n;
+    if (vec == 3) launch_spmv_nd<3, FMT_DF>(pat, n_nodes, hi, lo, xh, xl, y, nullptr, nullptr, 0, nullptr, 0, s);
+    else launch_spmv_nd<1, FMT_DF>(pat, n_nodes, hi, lo, xh, xl, y, nullptr, nullptr, 0, nullptr, 0, s);
+    return check_launch("spmv_df");
+  }
   if (precision == FEM_F32) {
     if (vec == 3) launch_spmv<3, float>(pat, n_nodes, (const float*)vals, (const float*)x, (float*)y, nullptr, nullptr, 0, nullptr, 0, s);
     else launch_spmv<1, float>(pat, n_nodes, (const float*)vals, (const float*)x, (float*)y, nullptr, nullptr, 0, nullptr, 0, s);
@@ -744,4 +1269,66 @@ extern "C" int fem_dot(int32_t precision, const void* x, const void* y, int64_t 
     dot_kernel<double><<<g, VTHREADS, 0, s>>>(n, (const double*)x, (const double*)y, w.ctl, w.partials, out);
   note_launches(1);
   return check_launch("dot");
+}
+
+extern "C" int fem_pcg_refined(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
+                               const void* vals32, int32_t pc_kind, const void* pc32, const fem_mesh_t* mesh,
+                               const fem_material_t* mat, const double* u_lin, const uint8_t* bc_mask,
+                               const double* b, double* x, double rtol, double atol, double delta, int64_t maxiter,
+                               void* ws, size_t ws_bytes, int64_t* iterations, int64_t* updates, double* res_norm,
+                               int32_t* status, void* stream) {
+  FEM_REQUIRE(precision == FEM_F32 || precision == FEM_DF48, "precision must be FEM_F32 or FEM_DF48");
+  int rc = check_pat(pat, n_nodes, vec, FEM_F32);
+  if (rc) return rc;
+  FEM_REQUIRE(vals32 && b && x && ws && mesh && mat, "NULL argument");
+  FEM_REQUIRE(mesh->n_nodes == n_nodes && mesh->vec == vec, "mesh does not match the pattern");
+  FEM_REQUIRE(pc_kind == FEM_PC_NONE || pc32, "preconditioner data NULL");
+  FEM_REQUIRE(pc_kind >= FEM_PC_NONE && pc_kind <= FEM_PC_BJACOBI, "bad pc_kind");
+  FEM_REQUIRE(rtol >= 0 && atol >= 0 && maxiter >= 0 && delta > 0 && delta < 1, "bad tolerances");
+  FEM_REQUIRE(ws_bytes >= krylov_ws_bytes(n_nodes * vec, FEM_F64), "workspace too small (fem_krylov_workspace FP64)");
+  cudaStream_t s = as_stream(stream);
+  const float* V = (const float*)vals32;
+  const float* P = (const float*)pc32;
+#define FEM_REF_CASE(VEC, PC)                                                                                   \
+  if (vec == VEC && pc_kind == PC)                                                                              \
+    return precision == FEM_DF48                                                                                \
+               ? pcg_df_impl<VEC, PC>(pat, n_nodes, vals32, P, mesh, mat, u_lin, bc_mask, b, x, rtol, atol, delta, \
+                                      maxiter, ws, iterations, updates, res_norm, status, s)                   \
+               : pcg_refined_impl<VEC, PC>(pat, n_nodes, V, P, mesh, mat, u_lin, bc_mask, b, x, rtol, atol, delta, \
+                                           maxiter, ws, iterations, updates, res_norm, status, s);
+  FEM_REF_CASE(3, FEM_PC_NONE)
+  FEM_REF_CASE(3, FEM_PC_JACOBI)
+  FEM_REF_CASE(3, FEM_PC_BJACOBI)
+  FEM_REF_CASE(1, FEM_PC_NONE)
+  FEM_REF_CASE(1, FEM_PC_JACOBI)
+  FEM_REF_CASE(1, FEM_PC_BJACOBI)
+#undef FEM_REF_CASE
+  return fail(FEM_ERR_ARG, "bad vec / preconditioner");
+}
+
+extern "C" int fem_matrix_bytes(int64_t nnz, int32_t precision, size_t* bytes) {
+  FEM_REQUIRE(bytes && nnz >= 0, "bad arguments");
+  if (precision == FEM_F32) *bytes = sizeof(float) * (size_t)nnz;
+  else if (precision == FEM_F64) *bytes = sizeof(double) * (size_t)nnz;
+  else if (precision == FEM_DF48) *bytes = df_lo_offset(nnz) + sizeof(int16_t) * (size_t)nnz;
+  else return fail(FEM_ERR_ARG, "bad precision");
+  return FEM_OK;
+}
+
+extern "C" int fem_matrix_split(const double* vals64, int64_t nnz, void* vals_df, void* stream) {
+  FEM_REQUIRE(nnz >= 0 && (nnz == 0 || (vals64 && vals_df)), "NULL argument");
+  if (nnz == 0) return FEM_OK;
+  float* hi = (float*)vals_df;
+  int16_t* lo = reinterpret_cast<int16_t*>((char*)vals_df + df_lo_offset(nnz));
+  split_df_kernel<<<grid_for(nnz, 256), 256, 0, as_stream(stream)>>>(vals64, nnz, hi, lo);
+  note_launches(1);
+  return check_launch("split_df");
+}
+
+extern "C" int fem_vector_split(const double* x, int64_t n, float* x_df, void* stream) {
+  FEM_REQUIRE(n >= 0 && (n == 0 || (x && x_df)), "NULL argument");
+  if (n == 0) return FEM_OK;
+  split_vec_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(x, n, x_df, x_df + n);
+  note_launches(1);
+  return check_launch("split_vec");
 }

@@ -26,11 +26,12 @@ class DeviceCSR:
 
     Stands where the reference passes a PETSc Mat (jax_fem/solver.py:540-553)."""
 
-    def __init__(self, eng, precision, vals, bc_mode):
+    def __init__(self, eng, precision, vals, bc_mode, source=None):
         self.eng = eng
         self.precision = precision
         self.data = vals
         self.bc_mode = bc_mode
+        self.source = source          # FP64 matrix a DF48 matrix was split from
         n = eng.num_dofs
         self.shape = (n, n)
         self.nnz = eng.nnz
@@ -49,6 +50,14 @@ class DeviceCSR:
         return self.eng.scalar_indices()
 
     def matvec(self, x):
+        if self.precision == _lib.FEM_DF48:
+            x = x.to(torch.float64).contiguous()
+            xs = torch.empty(2 * x.numel(), dtype=torch.float32, device=x.device)
+            call("fem_vector_split", ptr(x), x.numel(), ptr(xs), _stream())
+            y = torch.empty_like(x)
+            call("fem_spmv", C.byref(self.eng.pattern), self.eng.num_nodes, self.eng.vec, self.precision,
+                 ptr(self.data), ptr(xs), ptr(y), _stream())
+            return y
         x = x.to(self.data.dtype).contiguous()
         y = torch.empty_like(x)
         call("fem_spmv", C.byref(self.eng.pattern), self.eng.num_nodes, self.eng.vec, self.precision,
@@ -58,11 +67,21 @@ class DeviceCSR:
     __matmul__ = matvec
 
     def diagonal(self):
+        if self.source is not None:
+            return self.source.diagonal()
         return self.data[self.eng.diag]
 
     def preconditioner(self, kind):
         if kind == _lib.FEM_PC_NONE:
             return None
+        if self.source is not None:
+            # FP32 preconditioner of a DF48 matrix, set up from its FP64 source values
+            if kind not in self.pc:
+                pc64 = self.source.preconditioner(kind)
+                pc = torch.empty(pc64.numel(), dtype=torch.float32, device=pc64.device)
+                call("fem_cast_f64_f32", ptr(pc64), ptr(pc), pc64.numel(), None, _stream())
+                self.pc[kind] = pc
+            return self.pc[kind]
         if kind not in self.pc:
             n = self.eng.num_dofs if kind == _lib.FEM_PC_JACOBI else self.eng.num_nodes * self.eng.vec ** 2
             buf = torch.empty(n, dtype=self.data.dtype, device=self.data.device)
@@ -260,12 +279,26 @@ class Engine:
         return res
 
     def tangent(self, dofs, precision, bc_mode, cache=True):
-        """Assemble K(u) in `precision` with Dirichlet handling `bc_mode` and unit BC diagonal."""
+        """Assemble K(u) in `precision` with Dirichlet handling `bc_mode` and unit BC diagonal.
+        FEM_DF48 matrices are assembled in FP64 and split into the 6-byte double-float format."""
         self.refresh_bc()
         m, ms = self.material()
         key = (precision, bc_mode)
         if cache and m.linear and key in self._tangent_cache:
             return self._tangent_cache[key]
+        if precision == _lib.FEM_DF48:
+            A64 = self.tangent(dofs, _lib.FEM_F64, bc_mode, cache=cache)
+            nb = C.c_size_t()
+            call("fem_matrix_bytes", self.nnz, _lib.FEM_DF48, C.byref(nb))
+            buf = getattr(self, f"valsdf_{bc_mode}", None)
+            if buf is None or buf.numel() != nb.value:
+                buf = torch.empty(nb.value, dtype=torch.uint8, device=self.device)
+                setattr(self, f"valsdf_{bc_mode}", buf)
+            t0 = time.perf_counter()
+            call("fem_matrix_split", ptr(A64.data), self.nnz, ptr(buf), _stream())
+            A = DeviceCSR(self, _lib.FEM_DF48, buf, bc_mode, source=A64)
+            self._tangent_cache[key] = A
+            return A
         dtype = torch.float32 if precision == _lib.FEM_F32 else torch.float64
         buf_name = f"vals{precision}_{bc_mode}"
         vals = getattr(self, buf_name, None)
@@ -335,6 +368,28 @@ class Engine:
         self.solve_log.append(rec)
         logger.debug("krylov %s", rec)
         return it.value, rn.value, st.value
+
+    def pcg_refined(self, A32, b, x, u_lin, pc_kind, rtol, atol, delta, maxiter):
+        """PCG with FP64 reliable updates on the Dirichlet-eliminated tangent at u_lin; A32 is a
+        FEM_F32 or FEM_DF48 matrix.  x (FP64) is updated in place.
+        Returns (iterations, residual replacements, residual, status)."""
+        self.refresh_bc()
+        _, ms = self.material()
+        ws = self.workspace(_lib.FEM_F64)
+        pc = A32.preconditioner(pc_kind)
+        it, up, rn, st = C.c_int64(), C.c_int64(), C.c_double(), C.c_int32()
+        t0 = time.perf_counter()
+        call("fem_pcg_refined", C.byref(self.pattern), self.num_nodes, self.vec, A32.precision, ptr(A32.data),
+             pc_kind, ptr(pc),
+             C.byref(self.mesh), C.byref(ms), ptr(u_lin.contiguous()), ptr(self.bc_mask), ptr(b.contiguous()), ptr(x),
+             float(rtol), float(atol), float(delta), int(maxiter), ptr(ws), ws.numel(), C.byref(it), C.byref(up),
+             C.byref(rn), C.byref(st), _stream())
+        rec = dict(method="cg-refined", precision="df48+fp64" if A32.precision == _lib.FEM_DF48 else "fp32+fp64",
+                   iterations=it.value, updates=up.value,
+                   res_norm=rn.value, status=_lib.SOLVE_STATUS.get(st.value, "?"), seconds=time.perf_counter() - t0)
+        self.solve_log.append(rec)
+        logger.debug("krylov %s", rec)
+        return it.value, up.value, rn.value, st.value
 
     def cast32(self, x64, mask=None):
         out = torch.empty(x64.numel(), dtype=torch.float32, device=self.device)

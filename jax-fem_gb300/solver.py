@@ -30,7 +30,7 @@ from .logger import logger
 _METHOD_KEYS = frozenset({"newton", "arc_length", "dynamic_relax"})
 _LINEAR_OPTION_KEYS = frozenset({"jax_solver", "amgx_solver", "spsolve_solver", "petsc_solver", "custom_solver"})
 _NEWTON_OPTION_KEYS = frozenset({"tol", "rel_tol", "line_search_flag", "initial_guess", "precision", "inner_rtol",
-                                 "max_iter"})
+                                 "max_iter", "refine_delta"})
 
 
 def _resolve_solver_options(solver_options):
@@ -102,9 +102,13 @@ def resolve_linear(linear_options):
 
 def _precision(cfg):
     p = cfg.get("precision", "fp64")
-    if p not in ("fp64", "mixed"):
-        raise ValueError("precision must be 'fp64' or 'mixed'")
+    if p not in ("fp64", "mixed", "mixed32"):
+        raise ValueError("precision must be 'fp64', 'mixed' (DF48 matrix, FP64 vectors) or 'mixed32' (FP32)")
     return p
+
+
+def _mixed_matrix_precision(precision):
+    return _lib.FEM_DF48 if precision == "mixed" else _lib.FEM_F32
 
 
 def get_A(problem):
@@ -142,7 +146,9 @@ def _timed(eng, key, t0):
 def _newton_step(problem, eng, dofs, res, spec, precision, cfg):
     """One Newton correction A inc = -res (solver.py:390-421) with the Dirichlet rows of the
     increment equal to g - u_b."""
-    prec = _lib.FEM_F32 if precision == "mixed" else _lib.FEM_F64
+    prec = _lib.FEM_F64 if precision == "fp64" else _mixed_matrix_precision(precision)
+    if prec == _lib.FEM_DF48 and spec.method != "cg":
+        prec = _lib.FEM_F32          # BiCGStab mixed path runs in FP32 with Newton-level refinement
     eng.refresh_bc()
     rows = eng.bc_rows_long
     du_b = eng.bc_vals - dofs[rows] if eng.n_bc else None
@@ -174,7 +180,14 @@ def _newton_step(problem, eng, dofs, res, spec, precision, cfg):
             err = torch.linalg.norm(A.matvec(x) - b).item()      # solver.py:86-89
             assert err < 0.1, f"linear solver failed to converge with err = {err}"
         inc = x
+    elif spec.method == "cg":
+        # FP32 PCG with FP64 reliable updates: converges on the FP64 true residual
+        x = x0.clone()
+        it, up, rn, st = eng.pcg_refined(A, b, x, dofs, spec.pc, spec.rtol, spec.atol,
+                                         cfg.get("refine_delta", 0.1), spec.maxiter)
+        inc = x
     else:
+        # BiCGStab in FP32; the Newton loop's FP64 residual acts as the refinement
         b32 = eng.cast32(b)
         x32 = eng.cast32(x0)
         it, rn, st = eng.krylov(spec.method, A, b32, x32, spec.pc, inner, 0.0, spec.maxiter)
@@ -192,7 +205,10 @@ def _newton_step(problem, eng, dofs, res, spec, precision, cfg):
         if eng.n_bc:
             new[rows] = eng.bc_vals      # constraints hold exactly in FP64
         return new
-    return dofs + inc
+    new = dofs + inc
+    if prec != _lib.FEM_F64 and eng.n_bc:
+        new[rows] = eng.bc_vals
+    return new
 
 
 def _line_search(problem, eng, dofs, inc):
@@ -279,6 +295,7 @@ def adjoint_solve(problem, dofs, v, adjoint_solver_options=None, precision="fp64
     opts = dict(adjoint_solver_options or {})
     prec_opt = opts.pop("precision", precision)
     inner_rtol = opts.pop("inner_rtol", inner_rtol)
+    refine_delta = opts.pop("refine_delta", 0.1)
     spec = resolve_linear(opts)
     eng.refresh_bc()
     b = v.clone()
@@ -294,8 +311,13 @@ def adjoint_solve(problem, dofs, v, adjoint_solver_options=None, precision="fp64
         eng.krylov(spec.method, A, b, lam, spec.pc, spec.rtol, spec.atol, spec.maxiter)
         _timed(eng, "linear", t0)
         return lam
-    A = eng.tangent(dofs, _lib.FEM_F32, _lib.FEM_BC_SYMMETRIC)
+    mprec = _mixed_matrix_precision(prec_opt) if spec.method == "cg" else _lib.FEM_F32
+    A = eng.tangent(dofs, mprec, _lib.FEM_BC_SYMMETRIC)
     lam = torch.zeros_like(b)
+    if spec.method == "cg":
+        eng.pcg_refined(A, b, lam, dofs, spec.pc, spec.rtol, spec.atol, refine_delta, spec.maxiter)
+        _timed(eng, "linear", t0)
+        return lam
     r = b
     bn = torch.linalg.norm(b).item()
     if bn == 0.0:

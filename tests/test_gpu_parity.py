@@ -342,3 +342,30 @@ def test_maxiter_status(cuda):
     x = torch.zeros_like(b)
     it, rn, st = eng.krylov("cg", A, b, x, jf._lib.FEM_PC_JACOBI, 1e-14, 0.0, 3)
     assert it == 3 and st == jf._lib.FEM_SOLVE_MAXITER
+
+
+def test_df48_spmv_matches_fp64(cuda):
+    """DF48 (FP32 hi + int16 correction, double-float SpMV) reproduces the FP64 SpMV to ~1e-11."""
+    import jax_fem_gb300 as jf
+    import cases
+    prob, _, theta_np = cases.simp_box(10, 5, 3)
+    prob.set_params(torch.tensor(theta_np, device=cuda))
+    eng = prob._engine
+    z = torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda)
+    A64 = eng.tangent(z, jf._lib.FEM_F64, jf._lib.FEM_BC_SYMMETRIC, cache=False)
+    Adf = eng.tangent(z, jf._lib.FEM_DF48, jf._lib.FEM_BC_SYMMETRIC, cache=False)
+    x = torch.randn(eng.num_dofs, dtype=torch.float64, device=cuda)
+    y64 = A64.matvec(x)
+    ydf = Adf.matvec(x)
+    assert (ydf - y64).abs().max().item() <= 1e-11 * y64.abs().max().item()
+
+
+def test_mixed32_variant_converges(cuda):
+    """The all-FP32 variant (FP32 matrix and vectors, FP64 reliable updates) meets the same tolerance."""
+    import cases
+    prob, _, theta_np = cases.simp_box(12, 6, 3)
+    o = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-10}, "rel_tol": 1e-10, "tol": 0.0}
+    s64, J64, g64 = _simp_grad(prob, theta_np, cuda, o, o)
+    s32, J32, g32 = _simp_grad(prob, theta_np, cuda, dict(o, precision="mixed32"), dict(o, precision="mixed32"))
+    assert (s32 - s64).abs().max().item() <= 1e-8 * s64.abs().max().item()
+    assert np.abs(g32 - g64).max() <= 1e-7 * np.abs(g64).max()
