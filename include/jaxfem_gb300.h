@@ -207,6 +207,19 @@ int fem_pcg(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t prec
             const void* vals, int32_t pc_kind, const void* pc, const void* b, void* x,
             double rtol, double atol, int64_t maxiter, void* ws, size_t ws_bytes,
             int64_t* iterations, double* res_norm, int32_t* status, void* stream);
+/* Allocation-free PCG (no counterpart in the reference).  Same method, arguments and result
+ * as fem_pcg, for callers that cannot allocate device memory: code running while a stream is
+ * captured into a CUDA graph, host frameworks whose allocator is closed to plug-ins, embeddings
+ * that forbid allocation after start-up.  Its scratch is a fixed file-scope device array of
+ * about 8.6 MB that every GPU loading the library keeps until the process exits; systems of
+ * more than 262144 dofs (n_nodes*vec) are rejected with FEM_ERR_CAPACITY.  The first call on a
+ * device looks up the array's device address (make that first call before any stream capture).
+ * Every call shares the array, so calls that overlap on the GPU (two streams, two threads)
+ * race: serialise them.  Allocates nothing (no cudaMalloc / cudaFree).  Syncs. */
+int fem_pcg_static(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
+                   const void* vals, int32_t pc_kind, const void* pc, const void* b, void* x,
+                   double rtol, double atol, int64_t maxiter, int64_t* iterations, double* res_norm,
+                   int32_t* status, void* stream);
 /* BiCGStab with jax.scipy.sparse.linalg.bicgstab's iteration and stopping rule
  * ||r||^2 <= max(tol^2 ||b||^2, atol^2) (solver.py:78-84).  Syncs. */
 int fem_bicgstab(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,

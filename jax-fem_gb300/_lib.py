@@ -79,6 +79,7 @@ SIGNATURES = {
     "fem_precond_setup": ([PPAT, I64, I32, I32, P, I32, P, P], C.c_int),
     "fem_krylov_workspace": ([I64, I32, PSZ], C.c_int),
     "fem_pcg": ([PPAT, I64, I32, I32, P, I32, P, P, P, F64, F64, I64, P, SZ, PI64, PF64, PI32, P], C.c_int),
+    "fem_pcg_static": ([PPAT, I64, I32, I32, P, I32, P, P, P, F64, F64, I64, PI64, PF64, PI32, P], C.c_int),
     "fem_bicgstab": ([PPAT, I64, I32, I32, P, I32, P, P, P, F64, F64, I64, P, SZ, PI64, PF64, PI32, P], C.c_int),
     "fem_pcg_refined": ([PPAT, I64, I32, I32, P, I32, P, PMESH, PMAT, P, P, P, P, F64, F64, F64, I64, P, SZ, PI64,
                          PI64, PF64, PI32, P], C.c_int),

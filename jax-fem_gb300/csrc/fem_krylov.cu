@@ -16,6 +16,7 @@
 // first iteration meeting the criterion.  The host polls `done` every CHUNK
 // iterations; no kernel ever waits on another.
 #include <cmath>
+#include <mutex>
 
 #include "fem_common.cuh"
 #include "fem_elements.cuh"
@@ -1331,4 +1332,69 @@ extern "C" int fem_vector_split(const double* x, int64_t n, float* x_df, void* s
   split_vec_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(x, n, x_df, x_df + n);
   note_launches(1);
   return check_launch("split_vec");
+}
+
+// ---- allocation-free PCG ----------------------------------------------------------
+// For callers that cannot allocate device memory themselves -- code running while a
+// stream is being captured into a CUDA graph (allocation calls are not capturable), a
+// host framework whose allocator is closed to plug-ins, or an embedding that forbids
+// runtime allocation after start-up -- fem_pcg_static runs the same PCG as fem_pcg with
+// its scratch (control block, per-CTA partial sums, four Krylov vectors) in this
+// file-scope device array.  Every GPU that loads the library holds the array until the
+// process exits; every call shares it.
+namespace fem {
+constexpr int64_t STATIC_PCG_MAX_DOFS = 262144;
+constexpr size_t al_c(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t STATIC_PCG_BYTES = al_c(sizeof(KCtl)) + al_c(sizeof(double) * 3 * MAX_PARTIAL_BLOCKS) +
+                                    4 * al_c(sizeof(double) * STATIC_PCG_MAX_DOFS);
+__device__ __align__(256) unsigned char g_static_pcg_scratch[STATIC_PCG_BYTES];
+
+// Device address of the scratch array on the current device, looked up once per device.
+// The host-side name g_static_pcg_scratch is only a stand-in for the symbol and is never
+// passed to a kernel.
+static int static_pcg_scratch(void** out) {
+  static std::mutex mu;
+  static void* addr[128] = {};
+  int dev = 0;
+  FEM_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 128) return fail(FEM_ERR_ARG, "device ordinal out of range");
+  std::lock_guard<std::mutex> lk(mu);
+  if (addr[dev] == nullptr) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_pcg_scratch);
+    if (e != cudaSuccess || p == nullptr)
+      return fail(FEM_ERR_CUDA, std::string("cudaGetSymbolAddress(g_static_pcg_scratch): ") + cudaGetErrorString(e));
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return FEM_OK;
+}
+}  // namespace fem
+
+extern "C" int fem_pcg_static(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
+                              const void* vals, int32_t pc_kind, const void* pc, const void* b, void* x,
+                              double rtol, double atol, int64_t maxiter, int64_t* iterations, double* res_norm,
+                              int32_t* status, void* stream) {
+  int rc = check_pat(pat, n_nodes, vec, precision);
+  if (rc) return rc;
+  if (n_nodes * vec > STATIC_PCG_MAX_DOFS)
+    return fail(FEM_ERR_CAPACITY, "fem_pcg_static: " + std::to_string(n_nodes * vec) +
+                                      " dofs exceed its fixed scratch limit of " +
+                                      std::to_string(STATIC_PCG_MAX_DOFS) +
+                                      " dofs; use fem_pcg with a caller workspace");
+  FEM_REQUIRE(vals && b && x, "NULL argument");
+  FEM_REQUIRE(pc_kind == FEM_PC_NONE || pc, "preconditioner data NULL");
+  FEM_REQUIRE(pc_kind >= FEM_PC_NONE && pc_kind <= FEM_PC_BJACOBI, "bad pc_kind");
+  FEM_REQUIRE(rtol >= 0 && atol >= 0 && maxiter >= 0, "tolerances / maxiter must be non-negative");
+  void* ws = nullptr;
+  rc = static_pcg_scratch(&ws);
+  if (rc) return rc;
+  // the control block (done flag, tickets, scalars) is reset by the solver's first kernel;
+  // partial sums and vectors are written before they are read, so nothing else is cleared
+  cudaStream_t s = as_stream(stream);
+  if (precision == FEM_F32)
+    return solve_dispatch<float>(false, pat, n_nodes, vec, vals, pc_kind, pc, b, x, rtol, atol, maxiter, ws,
+                                 iterations, res_norm, status, s);
+  return solve_dispatch<double>(false, pat, n_nodes, vec, vals, pc_kind, pc, b, x, rtol, atol, maxiter, ws,
+                                iterations, res_norm, status, s);
 }
