@@ -152,8 +152,10 @@ def run_steps(prob, fwd, theta, J_out=None):
 
 def spmv_roofline(prob, peak):
     """Time each cached SpMV format with CUDA events on the launching stream (direct C-ABI calls,
-    input vector prepared once).  Algorithmic bytes per launch: values (6 B/nnz DF48, 8 B FP64,
-    4 B FP32) + one 4-byte block column per vec*vec values + block_ptr + x read + y write."""
+    input vector prepared once).  DF48 is timed through fem_spmv_dfx, the kernel the mixed CG
+    runs (node-interleaved double-float x, double-float y, fused dot).  Algorithmic bytes per
+    launch: values (6 B/nnz DF48, 8 B FP64, 4 B FP32) + one 4-byte block column per vec*vec
+    values + slice or row pointers + x read + y write."""
     import ctypes as C
     import torch
     import jax_fem_gb300 as jf
@@ -161,22 +163,34 @@ def spmv_roofline(prob, peak):
     eng = prob._engine
     out = {}
     n, nnz, nnzb = eng.num_dofs, eng.nnz, eng.nnzb
-    fmts = ((jf._lib.FEM_DF48, "df48", 6, 8, 8), (jf._lib.FEM_F32, "fp32", 4, 4, 4), (jf._lib.FEM_F64, "fp64", 8, 8, 8))
+    L_ = jf._lib
+    fmts = ((L_.FEM_SLICED_DF48, "df48", 6, 8, 8), (L_.FEM_SLICED_F32, "fp32", 4, 4, 4),
+            (L_.FEM_SLICED_F64, "fp64", 8, 8, 8))
     for prec, name, es, xs, ys in fmts:
         A = eng._tangent_cache.get((prec, jf._lib.FEM_BC_SYMMETRIC))
         if A is None:
             continue
-        if prec == jf._lib.FEM_DF48:
-            x = torch.randn(2 * n, dtype=torch.float32, device="cuda")
-            y = torch.empty(n, dtype=torch.float64, device="cuda")
-        else:
-            x = torch.randn(n, dtype=A.data.dtype, device="cuda")
-            y = torch.empty_like(x)
-        s = torch.cuda.current_stream()
+        if prec == L_.FEM_SLICED_DF48:
+            pad = 4 if eng.vec == 3 else 1
+            x = torch.zeros(eng.num_nodes, pad, 2, dtype=torch.float32, device="cuda")
+            x[:, :eng.vec, 0] = torch.randn(eng.num_nodes, eng.vec, device="cuda")
+            yh = torch.empty(n, dtype=torch.float32, device="cuda")
+            yl = torch.empty_like(yh)
+            nb = C.c_size_t()
+            call("fem_krylov_workspace", n, prec, C.byref(nb))
+            ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
 
-        def launch():
-            call("fem_spmv", C.byref(eng.pattern), eng.num_nodes, eng.vec, prec, ptr(A.data), ptr(x), ptr(y),
-                 stream_handle())
+            def launch():
+                call("fem_spmv_dfx", C.byref(eng.pattern), eng.num_nodes, eng.vec, ptr(A.data), ptr(x), ptr(yh),
+                     ptr(yl), None, ptr(ws), nb.value, stream_handle())
+        else:
+            x = torch.randn(n, dtype=A.vector_dtype, device="cuda")
+            y = torch.empty_like(x)
+
+            def launch():
+                call("fem_spmv", C.byref(eng.pattern), eng.num_nodes, eng.vec, prec, ptr(A.data), ptr(x), ptr(y),
+                     stream_handle())
+        s = torch.cuda.current_stream()
         for _ in range(3):
             launch()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
@@ -412,7 +426,7 @@ def main():
         "data": "synthetic",
         "config": {"workload": name, "precision": "mixed", "tolerance": RTOL,
                    "solver": "block-Jacobi PCG, DF48 SpMV + FP64 vectors, FP64 reliable updates (true residual)",
-                   "l2": "inputs larger than L2 (FP32 CSR values alone are 0.98 GB > 129 MB)",
+                   "l2": "inputs larger than L2 (the DF48 matrix alone is 1.5 GB > 129 MB)",
                    "replicas": "one independent problem per GPU (no data-path collective)"},
         "pcg_iterations": its_mx,
         "phases_s": {k: v / args.steps for k, v in phases_mx.items()},
@@ -420,7 +434,7 @@ def main():
         "e2e": {"value": t_e2e / args.steps / world, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": f32.get("achieved_gbs"), "peak": peak, "unit": "GB/s",
                      "frac": f32.get("frac"), "traffic": traffic,
-                     "kernel": "spmv_kernel<3,FMT_DF> (fem_spmv FEM_DF48, double-float on FP32 pipes)",
+                     "kernel": "spmv_sliced_dfdf_bulk_kernel<3> (fem_spmv_dfx: FEM_SLICED_DF48, bulk-copy staged, double-float on FP32 pipes)",
                      "peak_kind": peak_kind, "algorithmic_bytes": f32.get("algorithmic_bytes"),
                      "launch_seconds": f32.get("seconds"), "fp64": roof.get("fp64"), "fp32": roof.get("fp32")},
         "cpu_baseline": cpu,

@@ -45,11 +45,19 @@ enum { FEM_HEX8 = 1, FEM_TET10 = 2, FEM_TET4 = 3 };          /* jax_fem/basis.py
 enum {
   FEM_F32 = 0,
   FEM_F64 = 1,
-  FEM_DF48 = 2   /* matrix values as FP32 hi + int16 correction q (a = hi + q*ulp(hi)/2^16, a
-                    40-bit mantissa in 6 bytes): hi[nnz] floats, then at byte offset
-                    round_up(4*nnz, 256) q[nnz] int16.  Vectors for FEM_DF48 SpMV: x is the
+  FEM_DF48 = 2,  /* matrix values as FP32 hi + int16 correction q (a = hi + q*ulp(hi)/2^16, a
+                    40-bit mantissa in 6 bytes): hi[m] floats, then at byte offset
+                    round_up(4*m, 256) q[m] int16.  Vectors for DF48 SpMV: x is the
                     (hi[n], lo[n]) float pair of fem_vector_split, y is FP64.  Arithmetic is
                     double-float on FP32 pipes (error-free two-product / two-sum). */
+  /* Sliced node-block layouts (solver copies; built by fem_matrix_convert from FP64 CSR
+   * values): node rows in slices of 32, slice s owning block slots slice_ptr[s] ..
+   * slice_ptr[s+1]; value v (= r*vec + d) of slot k for the node in lane l sits at
+   * (k*vec*vec + v)*32 + l.  One warp per slice, one lane per node row, every load a
+   * full coalesced line and no cross-lane reduction.  Vectors as for the unsliced type. */
+  FEM_SLICED_F32 = 3,
+  FEM_SLICED_F64 = 4,
+  FEM_SLICED_DF48 = 5
 };
 enum {                                                       /* built-in tensor maps     */
   FEM_MAT_LAPLACE = 1,        /* consts: [k]                      test_linear_poisson.py:15-17 */
@@ -87,6 +95,10 @@ typedef struct fem_pattern_t {
   const int64_t* indptr;    /* scalar CSR row pointers (n_nodes*vec+1)            */
   const int64_t* diag;      /* (n_nodes*vec) offset of each row's diagonal entry  */
   const uint8_t* slots;     /* (n_cells, npc, npc): position of conn[b] in row conn[a] */
+  int64_t n_slices;         /* sliced layout (fem_pattern_slices); 0 when not built  */
+  int64_t n_slots;          /* total block slots of the sliced layout (host value)    */
+  const int64_t* slice_ptr; /* (n_slices+1) first block slot of each 32-node slice    */
+  const int32_t* slice_cols;/* (n_slots*32) block column of slot k, lane l (padding: 0) */
 } fem_pattern_t;
 
 typedef struct fem_material_t {
@@ -191,12 +203,28 @@ int fem_apply_bc_vec(double* res, const double* dofs, const int32_t* rows, const
  * and PETSc KSPCG/KSPBCGS with PCJACOBI / PCBJACOBI (solver.py:109-134). */
 int fem_spmv(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
              const void* vals, const void* x, void* y, void* stream);
-/* Bytes of a value buffer of nnz entries in `precision` (FEM_F32 / FEM_F64 / FEM_DF48). */
-int fem_matrix_bytes(int64_t nnz, int32_t precision, size_t* bytes);
-/* FP64 values -> FEM_DF48 buffer (fem_matrix_bytes(nnz, FEM_DF48)). */
-int fem_matrix_split(const double* vals64, int64_t nnz, void* vals_df, void* stream);
+/* Sliced layout of the pattern: with slice_cols == NULL writes slice_ptr (n_slices+1, where
+ * n_slices = ceil(n_nodes/32)) and the slot count (host; syncs); otherwise fills slice_cols. */
+int fem_pattern_slices(int64_t n_nodes, const int64_t* block_ptr, const int32_t* block_cols,
+                       int64_t* slice_ptr, int32_t* slice_cols, int64_t* n_slots, void* stream);
+/* Bytes of a value buffer for `pat` in `precision` (any FEM_F32 .. FEM_SLICED_DF48). */
+int fem_matrix_bytes(const fem_pattern_t* pat, int32_t vec, int32_t precision, size_t* bytes);
+/* FP64 CSR values -> values in `precision` (FEM_F32, FEM_DF48 or a sliced type). */
+int fem_matrix_convert(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, const double* vals64,
+                       int32_t precision, void* out, void* stream);
 /* FP64 vector -> (hi[n], lo[n]) float pair, the FEM_DF48 SpMV input. */
 int fem_vector_split(const double* x, int64_t n, float* x_df, void* stream);
+/* The mixed CG's SpMV (no counterpart in the reference: the inner operator of
+ * fem_pcg_refined with FEM_SLICED_DF48).  y = A x with A in FEM_SLICED_DF48; x is a
+ * node-interleaved double-float vector: component c of node i is the float pair
+ * (hi, lo) at pair index i*pad + c, pad = 4 for vec 3 (32 bytes per node) and 1 for vec 1;
+ * y is written as y_hi[n] + y_lo[n] (scalar row order).  When xy_dot (device) is non-NULL it
+ * receives the dot x.y.  ws: at least fem_krylov_workspace(n_dofs, FEM_SLICED_DF48) bytes.
+ * For vec 3 with 16-byte aligned vals and slice_cols the slices are streamed through
+ * shared memory by bulk copies (cp.async.bulk + mbarrier); a barrier wait that exceeds
+ * its limit returns FEM_ERR_DEVICE. */
+int fem_spmv_dfx(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, const void* vals, const void* x_df,
+                 float* y_hi, float* y_lo, double* xy_dot, void* ws, size_t ws_bytes, void* stream);
 /* Jacobi: pc = 1/diag (n_dofs values); block Jacobi: inverse node blocks (n_nodes*vec*vec). */
 int fem_precond_setup(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
                       const void* vals, int32_t pc_kind, void* pc, void* stream);
@@ -227,21 +255,23 @@ int fem_bicgstab(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t
                  double tol, double atol, int64_t maxiter, void* ws, size_t ws_bytes,
                  int64_t* iterations, double* res_norm, int32_t* status, void* stream);
 
-/* Mixed-precision PCG with FP64 reliable updates.  precision FEM_F32: FP32 matrix, FP32
- * vectors; FEM_DF48: DF48 matrix (double-float SpMV on FP32 pipes), FP64 vectors and dots.
- * The preconditioner pc32 is FP32 in both cases.
+/* Mixed-precision PCG with FP64 reliable updates.  precision FEM_F32 / FEM_SLICED_F32: FP32
+ * matrix, FP32 vectors; FEM_DF48 / FEM_SLICED_DF48: DF48 matrix (double-float SpMV on FP32
+ * pipes), FP64 vectors and dots.  The preconditioner pc32 is FP32 in all cases.
  * Solves the Dirichlet-eliminated system K_ff x_f = b_f (x_b = b_b on Dirichlet dofs)
  * where K is the tangent of `mat` at u_lin.  x (FP64, in/out) holds the initial guess.
  * When the FP32 recursive residual has fallen by `delta` since the last replacement,
  * the FP32 increment is added into x in FP64 and the residual is replaced by the true
- * residual b - K x computed in FP64 by the matrix-free tangent action; the search
- * direction is kept.  Stops when the FP64 true residual satisfies
+ * residual b - K x computed in FP64 -- by SpMV with vals_ref (the FP64 Dirichlet-eliminated
+ * matrix, FEM_F64 or FEM_SLICED_F64) when given, else by the matrix-free tangent action of
+ * mesh / mat at u_lin; the search direction is kept.  Stops when the FP64 true residual satisfies
  * ||b - K x||_2 <= max(rtol ||b||_2, atol).  ws >= fem_krylov_workspace(n, FEM_F64).
  * Replaces the reference's FP64-only linear solve in newton_step / implicit_vjp
  * (jax_fem/solver.py:390-421, 1399-1409) for the mixed-precision path.  Syncs. */
 int fem_pcg_refined(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision, const void* vals32,
                     int32_t pc_kind, const void* pc32, const fem_mesh_t* mesh, const fem_material_t* mat,
-                    const double* u_lin, const uint8_t* bc_mask, const double* b, double* x,
+                    const double* u_lin, const void* vals_ref, int32_t ref_precision,
+                    const uint8_t* bc_mask, const double* b, double* x,
                     double rtol, double atol, double delta, int64_t maxiter, void* ws, size_t ws_bytes,
                     int64_t* iterations, int64_t* updates, double* res_norm, int32_t* status, void* stream);
 

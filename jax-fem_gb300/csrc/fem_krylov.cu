@@ -32,9 +32,14 @@ struct KCtl {
   double rho, rho_prev, alpha, beta, omega, thresh2, rr, bb, d0, d1, ss;
   double rmax2, delta2, rr_true, check2;   // reliable-update PCG
   long long iter, maxiter;
-  int done, status, exit_early, pad;
+  int done, status, exit_early, fault;   // fault: a bounded device wait ran out
   unsigned int ticket[4];
 };
+
+static bool is_sliced(int p) { return p == FEM_SLICED_F32 || p == FEM_SLICED_F64 || p == FEM_SLICED_DF48; }
+static bool is_df(int p) { return p == FEM_DF48 || p == FEM_SLICED_DF48; }
+// FP32 vectors for FP32 matrices, FP64 vectors otherwise
+static bool vec_f32(int p) { return p == FEM_F32 || p == FEM_SLICED_F32; }
 
 // internal status: the FP32 iteration paused for an FP64 residual replacement
 constexpr int SOLVE_UPDATE = 10;
@@ -207,6 +212,46 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& err) 
   err = (a - (s - bb)) + (b - bb);
 }
 
+// ---- double-float CG recurrence (all vector arithmetic on FP32 pipes) ----------------
+// A df value is an unevaluated float pair h + l with |l| <= ulp(h)/2 (~48-bit mantissa).
+// GB300's FP64 pipe is ~1/64 of its FP32 rate, so the mixed solver keeps x, r, p, q in this
+// form and touches FP64 only to finish per-thread dot partials and in the scalar recurrences.
+struct df2 { float h, l; };
+
+__device__ __forceinline__ df2 df_fast(float s, float e) {  // |s| >= |e|
+  const float h = s + e;
+  return df2{h, e - (h - s)};
+}
+__device__ __forceinline__ df2 df_add(df2 a, df2 b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  e += a.l + b.l;
+  return df_fast(s, e);
+}
+__device__ __forceinline__ df2 df_mul(df2 a, df2 b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return df_fast(p, e);
+}
+__device__ __forceinline__ df2 df_of(double d) {
+  const float h = __double2float_rn(d);
+  return df2{h, __double2float_rn(d - (double)h)};
+}
+__device__ __forceinline__ double df_dbl(df2 a) { return (double)a.h + (double)a.l; }
+// accumulate a*b into (sh, sl) without renormalising every step
+__device__ __forceinline__ void df_acc(float& sh, float& sl, df2 a, df2 b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  float t, te;
+  two_sum(sh, p, t, te);
+  sl += te + e;
+  sh = t;
+}
+
 template <int FMT>
 struct SpmvTypes;
 template <> struct SpmvTypes<FMT_F32> { using V = float; using X = float; using Y = float; };
@@ -324,6 +369,382 @@ spmv_kernel(int64_t n_nodes, const int64_t* __restrict__ bp, const int32_t* __re
     }
   }
   if constexpr (ND > 0) reduce_and_finalize<ND>(dv, C, op, partials, C->ticket + ticket_id, nullptr);
+}
+
+// Sliced SpMV: one warp per 32-node slice, one lane per node row, all vec*vec values of a
+// block slot per lane; every column-index and value load is one coalesced line.
+template <int VEC, int FMT, int ND>
+__global__ void __launch_bounds__(SPMV_THREADS)
+spmv_sliced_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* __restrict__ sp,
+                   const int32_t* __restrict__ scols, const typename SpmvTypes<FMT>::V* __restrict__ vals,
+                   const int16_t* __restrict__ vlo, const typename SpmvTypes<FMT>::X* __restrict__ x,
+                   const float* __restrict__ xlo, typename SpmvTypes<FMT>::Y* __restrict__ y,
+                   const typename SpmvTypes<FMT>::Y* __restrict__ a, KCtl* C, int op, double* partials,
+                   int ticket_id) {
+  using V = typename SpmvTypes<FMT>::V;
+  using X = typename SpmvTypes<FMT>::X;
+  using Y = typename SpmvTypes<FMT>::Y;
+  constexpr int VV = VEC * VEC;
+  if (C && C->done) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double dv[3] = {0.0, 0.0, 0.0};
+  for (int64_t s = warp; s < n_slices; s += nwarps) {
+    const int64_t i = s * 32 + lane;
+    const int64_t k0 = sp[s], k1 = sp[s + 1];
+    Y out[VEC];
+    if constexpr (FMT == FMT_DF) {
+      float sh[VEC], sl[VEC];
+#pragma unroll
+      for (int r = 0; r < VEC; ++r) { sh[r] = 0.0f; sl[r] = 0.0f; }
+#pragma unroll 2
+      for (int64_t k = k0; k < k1; ++k) {
+        const int64_t col = (int64_t)VEC * __ldg(scols + k * 32 + lane);
+        float xh[VEC], xl[VEC];
+#pragma unroll
+        for (int d = 0; d < VEC; ++d) { xh[d] = __ldg(x + col + d); xl[d] = __ldg(xlo + col + d); }
+        const int64_t vb = k * VV * 32 + lane;
+#pragma unroll
+        for (int v = 0; v < VV; ++v) {
+          const int r = v / VEC, d = v % VEC;
+          const float ah = __ldcs(vals + vb + v * 32);
+          const float sc = __int_as_float((__float_as_int(ah) & 0x7f800000) - (39 << 23));
+          const float al = (float)__ldcs(vlo + vb + v * 32) * sc;
+          const float p = ah * xh[d];
+          float err = fmaf(ah, xh[d], -p);
+          err = fmaf(ah, xl[d], err);
+          err = fmaf(al, xh[d], err);
+          float t, te;
+          two_sum(sh[r], p, t, te);
+          sl[r] += te + err;
+          sh[r] = t;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < VEC; ++r) out[r] = (double)sh[r] + (double)sl[r];
+    } else {
+      V acc[VEC];
+#pragma unroll
+      for (int r = 0; r < VEC; ++r) acc[r] = V(0);
+#pragma unroll 2
+      for (int64_t k = k0; k < k1; ++k) {
+        const int64_t col = (int64_t)VEC * __ldg(scols + k * 32 + lane);
+        X xv[VEC];
+#pragma unroll
+        for (int d = 0; d < VEC; ++d) xv[d] = __ldg(x + col + d);
+        const int64_t vb = k * VV * 32 + lane;
+#pragma unroll
+        for (int v = 0; v < VV; ++v) acc[v / VEC] += __ldcs(vals + vb + v * 32) * xv[v % VEC];
+      }
+#pragma unroll
+      for (int r = 0; r < VEC; ++r) out[r] = acc[r];
+    }
+    if (i < n_nodes) {
+#pragma unroll
+      for (int r = 0; r < VEC; ++r) {
+        const int64_t row = (int64_t)VEC * i + r;
+        y[row] = out[r];
+        if constexpr (ND >= 1) dv[0] += double(a[row]) * double(out[r]);
+        if constexpr (ND >= 2) dv[1] += double(out[r]) * double(out[r]);
+      }
+    }
+  }
+  if constexpr (ND > 0) reduce_and_finalize<ND>(dv, C, op, partials, C->ticket + ticket_id, nullptr);
+}
+
+// Node-interleaved double-float vector: node i's component c is (hi, lo) at xp[i * DF_PAD + c];
+// for VEC = 3 a node occupies 32 bytes (one sector, two float4 loads per gathered column).
+template <int VEC>
+struct DfNode {
+  static constexpr int PAD = VEC == 3 ? 4 : VEC;
+};
+
+template <int VEC>
+__device__ __forceinline__ void df_gather(const float2* __restrict__ xp, int64_t node, float* h, float* l) {
+  if constexpr (VEC == 3) {
+    const float4* p4 = reinterpret_cast<const float4*>(xp) + 2 * node;
+    const float4 u0 = __ldg(p4), u1 = __ldg(p4 + 1);
+    h[0] = u0.x; l[0] = u0.y; h[1] = u0.z; l[1] = u0.w; h[2] = u1.x; l[2] = u1.y;
+  } else {
+#pragma unroll
+    for (int d = 0; d < VEC; ++d) {
+      const float2 u = __ldg(xp + node * VEC + d);
+      h[d] = u.x; l[d] = u.y;
+    }
+  }
+}
+
+// Sliced DF48 SpMV with a node-interleaved double-float input xp, double-float output (yh, yl)
+// and the fused dot d0 = x.y accumulated in double-float per thread (the mixed CG's p.Ap).
+template <int VEC>
+__global__ void __launch_bounds__(SPMV_THREADS)
+spmv_sliced_dfdf_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* __restrict__ sp,
+                        const int32_t* __restrict__ scols, const float* __restrict__ vals,
+                        const int16_t* __restrict__ vlo, const float2* __restrict__ xp,
+                        float* __restrict__ yh, float* __restrict__ yl, KCtl* C, int op, double* partials) {
+  constexpr int PAD = DfNode<VEC>::PAD;
+  constexpr int VV = VEC * VEC;
+  if (C->done) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  float ds = 0.f, de = 0.f;
+  for (int64_t s = warp; s < n_slices; s += nwarps) {
+    const int64_t i = s * 32 + lane;
+    const int64_t k0 = sp[s], k1 = sp[s + 1];
+    float sh[VEC], sl[VEC];
+#pragma unroll
+    for (int r = 0; r < VEC; ++r) { sh[r] = 0.0f; sl[r] = 0.0f; }
+#pragma unroll 2
+    for (int64_t k = k0; k < k1; ++k) {
+      float xvh[VEC], xvl[VEC];
+      df_gather<VEC>(xp, __ldg(scols + k * 32 + lane), xvh, xvl);
+      const int64_t vb = k * VV * 32 + lane;
+#pragma unroll
+      for (int v = 0; v < VV; ++v) {
+        const int r = v / VEC, d = v % VEC;
+        const float ah = __ldcs(vals + vb + v * 32);
+        const float sc = __int_as_float((__float_as_int(ah) & 0x7f800000) - (39 << 23));
+        const float al = (float)__ldcs(vlo + vb + v * 32) * sc;
+        df_acc(sh[r], sl[r], df2{ah, al}, df2{xvh[d], xvl[d]});
+      }
+    }
+    if (i < n_nodes) {
+#pragma unroll
+      for (int r = 0; r < VEC; ++r) {
+        const int64_t row = (int64_t)VEC * i + r;
+        const df2 yv = df_fast(sh[r], sl[r]);
+        yh[row] = yv.h;
+        yl[row] = yv.l;
+        const float2 xo = xp[i * PAD + r];
+        df_acc(ds, de, df2{xo.x, xo.y}, yv);
+      }
+    }
+  }
+  double dv[3] = {(double)ds + (double)de, 0.0, 0.0};
+  reduce_and_finalize<1>(dv, C, op, partials, C->ticket, &C->d0);
+}
+
+// ---- bulk-copy (TMA engine) staging for the sliced DF48 SpMV -------------------------
+// A slice's values, corrections and block columns are contiguous runs in HBM (slot-major), so
+// each warp streams its slices through a ring of shared-memory stages with 1-D
+// cp.async.bulk copies completing on one mbarrier per stage.  Lane 0 issues; every lane waits
+// on the stage's phase.  The HBM stream no longer depends on the per-thread load queue, so a
+// warp keeps BULK_STAGES - 1 chunks in flight while it computes on the third.
+constexpr int BULK_WARPS = 4;      // warps per CTA
+constexpr int BULK_STAGES = 3;     // ring depth per warp
+constexpr int BULK_SLOTS = 2;      // block-column slots per stage
+constexpr long long BULK_WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz: a wait past this is a fault
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void async_proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait for a phase; false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const long long t0 = clock64();
+  for (int it = 0; it < (1 << 26); ++it) {
+    if (mbar_test(bar, parity)) return true;
+    if (clock64() - t0 > BULK_WAIT_CYCLES) break;
+  }
+  return false;
+}
+
+template <int VEC>
+struct BulkGeom {
+  static constexpr uint32_t VB = VEC * VEC * 32 * 4;  // value bytes per slot
+  static constexpr uint32_t LB = VEC * VEC * 32 * 2;  // correction bytes per slot
+  static constexpr uint32_t CB = 32 * 4;              // block-column bytes per slot
+  static constexpr uint32_t STAGE = BULK_SLOTS * (VB + LB + CB);
+  static constexpr uint32_t BAR_BYTES = 128;          // BULK_WARPS * BULK_STAGES barriers, padded
+  static constexpr uint32_t SMEM = BAR_BYTES + BULK_WARPS * BULK_STAGES * STAGE;
+};
+
+// Sliced DF48 SpMV, bulk-copy staged: same arithmetic and outputs as spmv_sliced_dfdf_kernel.
+// Requires 16-byte aligned vals, vlo and slice_cols (checked by the host launcher).
+template <int VEC>
+__global__ void __launch_bounds__(BULK_WARPS * 32)
+spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* __restrict__ sp,
+                             const int32_t* __restrict__ scols, const float* __restrict__ vals,
+                             const int16_t* __restrict__ vlo, const float2* __restrict__ xp,
+                             float* __restrict__ yh, float* __restrict__ yl, KCtl* C, int op, double* partials) {
+  using G = BulkGeom<VEC>;
+  constexpr int VV = VEC * VEC;
+  constexpr int PAD = DfNode<VEC>::PAD;
+  extern __shared__ __align__(128) unsigned char smem[];
+  if (C->done) return;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + wib * BULK_STAGES;
+  unsigned char* ring = smem + G::BAR_BYTES + (size_t)wib * BULK_STAGES * G::STAGE;
+  const int64_t warp = (int64_t)blockIdx.x * BULK_WARPS + wib;
+  const int64_t nwarps = (int64_t)gridDim.x * BULK_WARPS;
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < BULK_STAGES; ++j) mbar_init(bars + j, 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+
+  // producer cursor: next chunk to copy (all lanes track it; lane 0 issues)
+  int64_t ps = warp, pk = 0, pe = 0;
+  if (ps < n_slices) { pk = sp[ps]; pe = sp[ps + 1]; }
+  auto produce = [&](int stage) -> bool {
+    while (ps < n_slices && pk == pe) {
+      ps += nwarps;
+      if (ps < n_slices) { pk = sp[ps]; pe = sp[ps + 1]; }
+    }
+    if (ps >= n_slices) return false;
+    const int64_t cnt = pe - pk < BULK_SLOTS ? pe - pk : BULK_SLOTS;
+    if (lane == 0) {
+      unsigned char* st = ring + (size_t)stage * G::STAGE;
+      const uint32_t nb = (uint32_t)cnt;
+      async_proxy_fence();
+      mbar_expect_tx(bars + stage, nb * (G::VB + G::LB + G::CB));
+      bulk_load(st, vals + pk * VV * 32, nb * G::VB, bars + stage);
+      bulk_load(st + BULK_SLOTS * G::VB, vlo + pk * VV * 32, nb * G::LB, bars + stage);
+      bulk_load(st + BULK_SLOTS * (G::VB + G::LB), scols + pk * 32, nb * G::CB, bars + stage);
+    }
+    pk += cnt;
+    return true;
+  };
+
+  uint32_t parity = 0;  // bit j: phase parity to wait for on stage j
+  int inflight = 0;
+  for (int j = 0; j < BULK_STAGES; ++j) inflight += produce(j) ? 1 : 0;
+
+  bool fault = false;
+  float ds = 0.f, de = 0.f;
+  int stage = 0;
+  int64_t cs = warp, ck = 0, ce = 0;
+  if (cs < n_slices) { ck = sp[cs]; ce = sp[cs + 1]; }
+  float sh[VEC], sl[VEC];
+#pragma unroll
+  for (int r = 0; r < VEC; ++r) { sh[r] = 0.f; sl[r] = 0.f; }
+  while (cs < n_slices) {
+    if (ck < ce) {
+      const bool ok = mbar_wait(bars + stage, (parity >> stage) & 1u);
+      if (!__all_sync(0xffffffffu, ok)) { fault = true; break; }
+      parity ^= 1u << stage;
+      --inflight;
+      const unsigned char* st = ring + (size_t)stage * G::STAGE;
+      const float* sv = reinterpret_cast<const float*>(st);
+      const int16_t* sq = reinterpret_cast<const int16_t*>(st + BULK_SLOTS * G::VB);
+      const int32_t* sc = reinterpret_cast<const int32_t*>(st + BULK_SLOTS * (G::VB + G::LB));
+      const int cnt = ce - ck < BULK_SLOTS ? (int)(ce - ck) : BULK_SLOTS;
+      float xvh[BULK_SLOTS][VEC], xvl[BULK_SLOTS][VEC];
+#pragma unroll
+      for (int t = 0; t < BULK_SLOTS; ++t)
+        if (t < cnt) df_gather<VEC>(xp, sc[t * 32 + lane], xvh[t], xvl[t]);
+#pragma unroll
+      for (int t = 0; t < BULK_SLOTS; ++t) {
+        if (t < cnt) {
+#pragma unroll
+          for (int v = 0; v < VV; ++v) {
+            const int r = v / VEC, d = v % VEC;
+            const float ah = sv[(t * VV + v) * 32 + lane];
+            const float sc2 = __int_as_float((__float_as_int(ah) & 0x7f800000) - (39 << 23));
+            const float al = (float)sq[(t * VV + v) * 32 + lane] * sc2;
+            df_acc(sh[r], sl[r], df2{ah, al}, df2{xvh[t][d], xvl[t][d]});
+          }
+        }
+      }
+      __syncwarp();
+      inflight += produce(stage) ? 1 : 0;
+      stage = stage + 1 == BULK_STAGES ? 0 : stage + 1;
+      ck += cnt;
+    }
+    if (ck == ce) {  // slice finished: write its rows and the dot contribution
+      const int64_t i = cs * 32 + lane;
+      if (i < n_nodes) {
+#pragma unroll
+        for (int r = 0; r < VEC; ++r) {
+          const int64_t row = (int64_t)VEC * i + r;
+          const df2 yv = df_fast(sh[r], sl[r]);
+          yh[row] = yv.h;
+          yl[row] = yv.l;
+          const float2 xo = xp[i * PAD + r];
+          df_acc(ds, de, df2{xo.x, xo.y}, yv);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < VEC; ++r) { sh[r] = 0.f; sl[r] = 0.f; }
+      cs += nwarps;
+      if (cs < n_slices) { ck = sp[cs]; ce = sp[cs + 1]; }
+    }
+  }
+  if (fault) {
+    // let the copies already issued land (bounded) before the CTA's shared memory is released
+    for (int j = 0; j < inflight; ++j) {
+      (void)mbar_wait(bars + stage, (parity >> stage) & 1u);
+      parity ^= 1u << stage;
+      stage = stage + 1 == BULK_STAGES ? 0 : stage + 1;
+    }
+    if (lane == 0) {
+      atomicExch(&C->fault, 1);
+      atomicExch(&C->done, 1);
+    }
+  }
+  double dv[3] = {(double)ds + (double)de, 0.0, 0.0};
+  reduce_and_finalize<1>(dv, C, op, partials, C->ticket, &C->d0);
+}
+
+// FP64 CSR values -> sliced layout (FP64, FP32 or DF48 hi/lo), thread per (slice, lane).
+template <int VEC, int OUT>
+__global__ void to_sliced_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* bp, const int64_t* sp,
+                                 const double* v64, void* out, int16_t* lo) {
+  constexpr int VV = VEC * VEC;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_slices * 32; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = t >> 5;
+    const int l = (int)(t & 31);
+    const int64_t i = s * 32 + l;
+    const int64_t b0 = i < n_nodes ? bp[i] : 0;
+    const int nb = i < n_nodes ? (int)(bp[i + 1] - b0) : 0;
+    const int64_t w = sp[s + 1] - sp[s];
+    for (int64_t k = 0; k < w; ++k) {
+      for (int v = 0; v < VV; ++v) {
+        const int r = v / VEC, d = v % VEC;
+        const double a = k < nb ? v64[(int64_t)VV * b0 + (int64_t)r * VEC * nb + VEC * k + d] : 0.0;
+        const int64_t o = ((sp[s] + k) * VV + v) * 32 + l;
+        if (OUT == FEM_SLICED_F64) {
+          static_cast<double*>(out)[o] = a;
+        } else if (OUT == FEM_SLICED_F32) {
+          static_cast<float*>(out)[o] = (float)a;
+        } else {
+          const float h = __double2float_rn(a);
+          const int e = (__float_as_int(h) >> 23) & 0xFF;
+          int q = 0;
+          if (e > 39 && e < 255) {
+            double tq = rint(scalbn(a - (double)h, 166 - e));
+            tq = fmin(fmax(tq, -32767.0), 32767.0);
+            q = (int)tq;
+          }
+          static_cast<float*>(out)[o] = h;
+          lo[o] = (int16_t)q;
+        }
+      }
+    }
+  }
 }
 
 // DF48 split of an FP64 matrix: hi = fl32(a), q = round((a - hi) * 2^16 / ulp(hi)).
@@ -551,6 +972,97 @@ __global__ void pcgd_direction_kernel(int64_t n, double* p, const double* z, flo
   }
 }
 
+// first start / restart after a residual replacement: z = M r.h ; (first) p = z ; dots (r.z, r.r)
+template <int VEC, int PC>
+__global__ void pcgx_start_kernel(int64_t n_nodes, const float* rh, const float* rl, float* z, float2* pp,
+                                  const float* pc, int first, KCtl* C, double* partials) {
+  constexpr int PAD = DfNode<VEC>::PAD;
+  float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f;
+  GRID_STRIDE_NODES(i, n_nodes) {
+    float rv[VEC], zv[VEC];
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) rv[c] = rh[VEC * i + c];
+    precond<VEC, float, PC>(pc, i, rv, zv);
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) {
+      const int64_t k = VEC * i + c;
+      z[k] = zv[c];
+      if (first) pp[i * PAD + c] = make_float2(zv[c], 0.f);
+      const df2 r{rv[c], rl[k]};
+      df_acc(s0, e0, r, df2{zv[c], 0.f});
+      df_acc(s1, e1, r, r);
+    }
+  }
+  double dv[3] = {(double)s0 + (double)e0, (double)s1 + (double)e1, 0.0};
+  reduce_and_finalize<2>(dv, C, FIN_PCGR_START, partials, C->ticket + 1, nullptr);
+}
+
+// x += alpha p ; r -= alpha q ; z = M r.h ; dots (r.z, r.r)
+template <int VEC, int PC>
+__global__ void pcgx_update_kernel(int64_t n_nodes, float* xh, float* xl, float* rh, float* rl, float* z,
+                                   const float2* pp, const float* qh, const float* ql, const float* pc,
+                                   KCtl* C, double* partials, int op) {
+  constexpr int PAD = DfNode<VEC>::PAD;
+  if (C->done) return;
+  const df2 a = df_of(C->alpha);
+  const df2 na{-a.h, -a.l};
+  float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f;
+  GRID_STRIDE_NODES(i, n_nodes) {
+    float rv[VEC], zv[VEC];
+    df2 rr[VEC];
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) {
+      const int64_t k = VEC * i + c;
+      const float2 pv = pp[i * PAD + c];
+      const df2 p{pv.x, pv.y}, q{qh[k], ql[k]};
+      const df2 x = df_add(df2{xh[k], xl[k]}, df_mul(a, p));
+      xh[k] = x.h; xl[k] = x.l;
+      const df2 r = df_add(df2{rh[k], rl[k]}, df_mul(na, q));
+      rh[k] = r.h; rl[k] = r.l;
+      rr[c] = r;
+      rv[c] = r.h;
+    }
+    precond<VEC, float, PC>(pc, i, rv, zv);
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) {
+      z[VEC * i + c] = zv[c];
+      df_acc(s0, e0, rr[c], df2{zv[c], 0.f});
+      df_acc(s1, e1, rr[c], rr[c]);
+    }
+  }
+  double dv[3] = {(double)s0 + (double)e0, (double)s1 + (double)e1, 0.0};
+  reduce_and_finalize<2>(dv, C, op, partials, C->ticket + 1, nullptr);
+}
+
+// p = z + beta p (df), the SpMV input of the next iteration
+template <int VEC>
+__global__ void pcgx_direction_kernel(int64_t n_nodes, const float* z, float2* pp, const KCtl* C) {
+  constexpr int PAD = DfNode<VEC>::PAD;
+  if (C->done) return;
+  const df2 b = df_of(C->beta);
+  GRID_STRIDE_NODES(i, n_nodes) {
+#pragma unroll
+    for (int c = 0; c < VEC; ++c) {
+      const float2 pv = pp[i * PAD + c];
+      const df2 p = df_add(df2{z[VEC * i + c], 0.f}, df_mul(b, df2{pv.x, pv.y}));
+      pp[i * PAD + c] = make_float2(p.h, p.l);
+    }
+  }
+}
+
+// df <-> FP64 for the reliable updates: x64 = x (df) ; (r.h, r.l) = split(r64)
+__global__ void df_to_f64_kernel(int64_t n, const float* h, const float* l, double* out) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = (double)h[k] + (double)l[k];
+}
+__global__ void f64_to_df_kernel(int64_t n, const double* v, float* h, float* l) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const df2 d = df_of(v[k]);
+    h[k] = d.h;
+    l[k] = d.l;
+  }
+}
+
 // FP64 true residual r = b - A x (Dirichlet rows: b - x) and ||r||^2
 __global__ void refine_residual64_kernel(int64_t n, const double* b, const double* x, const double* ax,
                                          const uint8_t* bc, double* r, KCtl* C, double* partials) {
@@ -663,7 +1175,7 @@ __global__ void dot_kernel(int64_t n, const T* x, const T* y, KCtl* C, double* p
 
 __global__ void init_ctl_kernel(KCtl* C, double thresh2_rel, double atol2, long long maxiter) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
-    C->done = 0; C->status = 0; C->exit_early = 0;
+    C->done = 0; C->status = 0; C->exit_early = 0; C->fault = 0;
     C->thresh2 = thresh2_rel; C->d1 = atol2; C->maxiter = maxiter; C->iter = 0;
     C->ticket[0] = C->ticket[1] = C->ticket[2] = C->ticket[3] = 0;
   }
@@ -796,23 +1308,98 @@ static void launch_spmv_nd(const fem_pattern_t* pat, int64_t n_nodes, const void
   else launch_spmv_fmt<VEC, FMT, 2>(pat, n_nodes, vals, vlo, x, xlo, y, a, C, op, partials, s);
 }
 
+template <int VEC, int FMT, int ND>
+static void launch_spmv_sliced(const fem_pattern_t* pat, int64_t n_nodes, const void* vals, const int16_t* vlo,
+                               const void* x, const float* xlo, void* y, const void* a, KCtl* C, int op,
+                               double* partials, cudaStream_t s) {
+  using Tp = SpmvTypes<FMT>;
+  auto kern = spmv_sliced_kernel<VEC, FMT, ND>;
+  static int per_sm = 0;
+  if (per_sm == 0) per_sm = spmv_blocks_per_sm(kern);
+  const int64_t need = (pat->n_slices * 32 + SPMV_THREADS - 1) / SPMV_THREADS;
+  int64_t g = (int64_t)sm_count() * per_sm;
+  if (g > need) g = need;
+  if (g > MAX_PARTIAL_BLOCKS) g = MAX_PARTIAL_BLOCKS;
+  if (g < 1) g = 1;
+  kern<<<(unsigned)g, SPMV_THREADS, 0, s>>>(n_nodes, pat->n_slices, pat->slice_ptr, pat->slice_cols,
+                                             (const typename Tp::V*)vals, vlo, (const typename Tp::X*)x, xlo,
+                                             (typename Tp::Y*)y, (const typename Tp::Y*)a, C, op, partials, 0);
+  note_launches(1);
+}
+
+// One entry for every value format: mfmt is the FEM_* precision of `vals`.
+template <int VEC, int FMT>
+static void launch_spmv_any(const fem_pattern_t* pat, int64_t n_nodes, int mfmt, const void* vals, const int16_t* vlo,
+                            const void* x, const float* xlo, void* y, const void* a, KCtl* C, int op,
+                            double* partials, int nd, cudaStream_t s) {
+  if (mfmt >= FEM_SLICED_F32) {
+    if (nd == 0) launch_spmv_sliced<VEC, FMT, 0>(pat, n_nodes, vals, vlo, x, xlo, y, a, C, op, partials, s);
+    else if (nd == 1) launch_spmv_sliced<VEC, FMT, 1>(pat, n_nodes, vals, vlo, x, xlo, y, a, C, op, partials, s);
+    else launch_spmv_sliced<VEC, FMT, 2>(pat, n_nodes, vals, vlo, x, xlo, y, a, C, op, partials, s);
+  } else {
+    launch_spmv_nd<VEC, FMT>(pat, n_nodes, vals, vlo, x, xlo, y, a, C, op, partials, nd, s);
+  }
+}
+
 template <int VEC, typename T>
 static void launch_spmv(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, const T* x, T* y, const T* a,
-                        KCtl* C, int op, double* partials, int nd, cudaStream_t s) {
+                        KCtl* C, int op, double* partials, int nd, cudaStream_t s, int mfmt = -1) {
   constexpr int FMT = sizeof(T) == 4 ? FMT_F32 : FMT_F64;
-  launch_spmv_nd<VEC, FMT>(pat, n_nodes, vals, nullptr, x, nullptr, y, a, C, op, partials, nd, s);
+  if (mfmt < 0) mfmt = sizeof(T) == 4 ? FEM_F32 : FEM_F64;
+  launch_spmv_any<VEC, FMT>(pat, n_nodes, mfmt, vals, nullptr, x, nullptr, y, a, C, op, partials, nd, s);
 }
 
 static int poll(KCtl* C, cudaStream_t s, KCtl* host) {
   FEM_CUDA(cudaMemcpyAsync(host, C, sizeof(KCtl), cudaMemcpyDeviceToHost, s));
   FEM_CUDA(cudaStreamSynchronize(s));
+  if (host->fault) return fail(FEM_ERR_DEVICE, "a bounded device wait (bulk-copy barrier) ran out");
   return FEM_OK;
+}
+
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+// The mixed CG's SpMV: bulk-copy staged kernel for vec 3 when the streamed arrays are 16-byte
+// aligned, the register-streaming kernel otherwise.  Grid: resident CTAs, capped by the slices.
+template <int VEC>
+static void launch_dfdf(const fem_pattern_t* pat, int64_t n_nodes, const float* vhi, const int16_t* vlo,
+                        const float2* xp, float* yh, float* yl, KCtl* C, int op, double* partials, cudaStream_t s) {
+  const int64_t ns = pat->n_slices;
+  if (VEC == 3 && aligned16(vhi) && aligned16(vlo) && aligned16(pat->slice_cols)) {
+    auto kern = spmv_sliced_dfdf_bulk_kernel<VEC>;
+    constexpr int smem = (int)BulkGeom<VEC>::SMEM;
+    static int per_sm = 0;
+    if (per_sm == 0) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BULK_WARPS * 32, smem) != cudaSuccess ||
+          per_sm < 1)
+        per_sm = 1;
+    }
+    int64_t g = (int64_t)sm_count() * per_sm;
+    const int64_t need = (ns + BULK_WARPS - 1) / BULK_WARPS;
+    if (g > need) g = need;
+    if (g > MAX_PARTIAL_BLOCKS) g = MAX_PARTIAL_BLOCKS;
+    if (g < 1) g = 1;
+    kern<<<(unsigned)g, BULK_WARPS * 32, smem, s>>>(n_nodes, ns, pat->slice_ptr, pat->slice_cols, vhi, vlo, xp, yh,
+                                                    yl, C, op, partials);
+  } else {
+    auto kern = spmv_sliced_dfdf_kernel<VEC>;
+    static int per_sm = 0;
+    if (per_sm == 0) per_sm = spmv_blocks_per_sm(kern);
+    int64_t g = (int64_t)sm_count() * per_sm;
+    const int64_t need = (ns * 32 + SPMV_THREADS - 1) / SPMV_THREADS;
+    if (g > need) g = need;
+    if (g > MAX_PARTIAL_BLOCKS) g = MAX_PARTIAL_BLOCKS;
+    if (g < 1) g = 1;
+    kern<<<(unsigned)g, SPMV_THREADS, 0, s>>>(n_nodes, ns, pat->slice_ptr, pat->slice_cols, vhi, vlo, xp, yh, yl, C,
+                                              op, partials);
+  }
+  note_launches(1);
 }
 
 template <int VEC, typename T, int PC>
 static int pcg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, const T* pc, const T* b, T* x,
                     double rtol, double atol, int64_t maxiter, void* ws, int64_t* iters, double* rnorm,
-                    int32_t* status, cudaStream_t s) {
+                    int32_t* status, cudaStream_t s, int mfmt) {
   const int64_t n = n_nodes * VEC;
   KWs w = carve(ws, n, sizeof(T) == 4 ? FEM_F32 : FEM_F64);
   T* r = reinterpret_cast<T*>(w.vecs);
@@ -822,7 +1409,7 @@ static int pcg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, co
   KCtl* C = w.ctl;
   init_ctl_kernel<<<1, 32, 0, s>>>(C, rtol * rtol, atol * atol, (long long)maxiter);
   note_launches(1);
-  launch_spmv<VEC, T>(pat, n_nodes, vals, x, q, nullptr, nullptr, FIN_NONE, nullptr, 0, s);
+  launch_spmv<VEC, T>(pat, n_nodes, vals, x, q, nullptr, nullptr, FIN_NONE, nullptr, 0, s, mfmt);
   pcg_init_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, b, q, r, z, p, pc, C, w.partials);
   note_launches(1);
   int rc = check_launch("pcg init");
@@ -834,7 +1421,7 @@ static int pcg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, co
     if (rc) return rc;
     if (h.done || launched >= maxiter) break;
     for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
-      launch_spmv<VEC, T>(pat, n_nodes, vals, p, q, p, C, FIN_PCG_ALPHA, w.partials, 1, s);
+      launch_spmv<VEC, T>(pat, n_nodes, vals, p, q, p, C, FIN_PCG_ALPHA, w.partials, 1, s, mfmt);
       pcg_update_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, x, r, z, p, q, pc, C, w.partials,
                                                                             FIN_PCG_UPDATE);
       note_launches(1);
@@ -853,7 +1440,7 @@ static int pcg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, co
 template <int VEC, typename T, int PC>
 static int bicg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, const T* pc, const T* b, T* x,
                      double tol, double atol, int64_t maxiter, void* ws, int64_t* iters, double* rnorm,
-                     int32_t* status, cudaStream_t s) {
+                     int32_t* status, cudaStream_t s, int mfmt) {
   const int64_t n = n_nodes * VEC;
   KWs w = carve(ws, n, sizeof(T) == 4 ? FEM_F32 : FEM_F64);
   T* v[8];
@@ -862,7 +1449,7 @@ static int bicg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, c
   KCtl* C = w.ctl;
   init_ctl_kernel<<<1, 32, 0, s>>>(C, tol * tol, atol * atol, (long long)maxiter);
   note_launches(1);
-  launch_spmv<VEC, T>(pat, n_nodes, vals, x, q, nullptr, nullptr, FIN_NONE, nullptr, 0, s);
+  launch_spmv<VEC, T>(pat, n_nodes, vals, x, q, nullptr, nullptr, FIN_NONE, nullptr, 0, s, mfmt);
   bicg_init_kernel<T><<<vec_grid(n), VTHREADS, 0, s>>>(n, b, q, r, rhat, p, C, w.partials);
   note_launches(1);
   int rc = check_launch("bicgstab init");
@@ -876,10 +1463,10 @@ static int bicg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, c
     for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
       bicg_p_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, p, q, phat, pc, C);
       note_launches(1);
-      launch_spmv<VEC, T>(pat, n_nodes, vals, phat, q, rhat, C, FIN_BICG_ALPHA, w.partials, 1, s);
+      launch_spmv<VEC, T>(pat, n_nodes, vals, phat, q, rhat, C, FIN_BICG_ALPHA, w.partials, 1, s, mfmt);
       bicg_s_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, q, sv, shat, pc, C, w.partials);
       note_launches(1);
-      launch_spmv<VEC, T>(pat, n_nodes, vals, shat, t, sv, C, FIN_BICG_OMEGA, w.partials, 2, s);
+      launch_spmv<VEC, T>(pat, n_nodes, vals, shat, t, sv, C, FIN_BICG_OMEGA, w.partials, 2, s, mfmt);
       bicg_update_kernel<T><<<vec_grid(n), VTHREADS, 0, s>>>(n, x, r, rhat, phat, sv, shat, t, C, w.partials);
       note_launches(1);
     }
@@ -892,6 +1479,30 @@ static int bicg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, c
   return FEM_OK;
 }
 
+// FP64 operator of the reliable updates: an FP64 matrix (CSR or sliced) when given, else
+// the matrix-free tangent action of `mat` at u_lin.  ax := K x (Dirichlet-eliminated).
+struct RefOp {
+  const fem_mesh_t* mesh;
+  const fem_material_t* mat;
+  const double* u_lin;
+  const void* vals;
+  int prec;
+  const uint8_t* bc;
+};
+
+template <int VEC>
+static int ref_apply(const fem_pattern_t* pat, int64_t n_nodes, const RefOp& op, const double* x, double* ax,
+                     cudaStream_t s) {
+  if (op.vals) {
+    launch_spmv<VEC, double>(pat, n_nodes, (const double*)op.vals, x, ax, nullptr, nullptr, FIN_NONE, nullptr, 0, s,
+                             op.prec);
+    return check_launch("reliable-update SpMV");
+  }
+  FEM_CUDA(cudaMemsetAsync(ax, 0, sizeof(double) * (size_t)(n_nodes * VEC), s));
+  return fem_assemble(op.mesh, op.mat, pat, FEM_OUT_APPLY, FEM_F64, op.u_lin, x, op.bc, FEM_BC_SYMMETRIC, nullptr,
+                      nullptr, ax, s);
+}
+
 // FP32 PCG with FP64 reliable updates (residual replacement).  The iteration runs on
 // the FP32 matrix; whenever the FP32 recursive residual has fallen by `delta` since the
 // last replacement (or below a quarter of the target), the device pauses, the host adds
@@ -901,10 +1512,10 @@ static int bicg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, c
 // instead of restarting.  Convergence is declared only on the FP64 true residual.
 template <int VEC, int PC>
 static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const float* vals, const float* pc,
-                            const fem_mesh_t* mesh, const fem_material_t* mat, const double* u_lin,
-                            const uint8_t* bc, const double* b, double* x, double rtol, double atol, double delta,
+                            const RefOp& op, const double* b, double* x, double rtol, double atol, double delta,
                             int64_t maxiter, void* ws, int64_t* iters, int64_t* updates, double* rnorm,
-                            int32_t* status, cudaStream_t s) {
+                            int32_t* status, cudaStream_t s, int mfmt) {
+  const uint8_t* bc = op.bc;
   const int64_t n = n_nodes * VEC;
   KWs w = carve(ws, n, FEM_F64);
   const size_t f4 = al(sizeof(float) * (size_t)n);
@@ -921,9 +1532,7 @@ static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const flo
   int rc = check_launch("pcg_refined init");
   if (rc) return rc;
   auto true_residual = [&]() -> int {
-    FEM_CUDA(cudaMemsetAsync(ax, 0, sizeof(double) * (size_t)n, s));
-    const int r2 = fem_assemble(mesh, mat, pat, FEM_OUT_APPLY, FEM_F64, u_lin, x, bc, FEM_BC_SYMMETRIC, nullptr,
-                                nullptr, ax, s);
+    const int r2 = ref_apply<VEC>(pat, n_nodes, op, x, ax, s);
     if (r2) return r2;
     refine_residual_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(n, b, x, ax, bc, r, C, w.partials);
     note_launches(1);
@@ -980,7 +1589,7 @@ static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const flo
       }
       if (launched >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
       for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
-        launch_spmv<VEC, float>(pat, n_nodes, vals, p, q, p, C, FIN_PCG_ALPHA, w.partials, 1, s);
+        launch_spmv<VEC, float>(pat, n_nodes, vals, p, q, p, C, FIN_PCG_ALPHA, w.partials, 1, s, mfmt);
         pcg_update_kernel<VEC, float, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, x32, r, z, p, q, pc, C,
                                                                                 w.partials, FIN_PCGR_UPDATE);
         pcg_direction_kernel<float><<<vec_grid(n), VTHREADS, 0, s>>>(n, p, z, C);
@@ -1000,19 +1609,127 @@ static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const flo
 // Byte offset of the int16 corrections inside a DF48 value buffer.
 static inline size_t df_lo_offset(int64_t nnz) { return al(sizeof(float) * (size_t)nnz); }
 
+// Number of stored values of a matrix in `mfmt` (sliced layouts include their padding).
+static inline int64_t n_values(const fem_pattern_t* pat, int vec, int mfmt) {
+  if (mfmt >= FEM_SLICED_F32) return pat->n_slots * vec * vec * 32;
+  return pat->nnzb * vec * vec;
+}
+
 // DF48 PCG with FP64 reliable updates: FP64 CG vectors and dots, the matrix stream in the
 // 6-byte double-float format (SpMV on FP32 pipes, FP64-level accuracy), FP32 block-Jacobi.
 // The FP64 true residual (matrix-free tangent action) replaces the recursive residual
 // whenever it has fallen by `delta`, and is the only convergence test.
+// Double-float CG on the sliced DF48 matrix with FP64 reliable updates.  x, r, p, q live
+// as float pairs (FP32 pipes only); the FP64 true residual b - K x (matrix-free tangent
+// action) replaces r whenever the recursive residual has fallen by `delta`, and is the
+// only convergence test.  x (FP64, caller's buffer) is read at start and written back.
 template <int VEC, int PC>
-static int pcg_df_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* vals, const float* pc,
-                       const fem_mesh_t* mesh, const fem_material_t* mat, const double* u_lin, const uint8_t* bc,
+static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* vals, const float* pc, const RefOp& op,
+                        const double* b, double* x, double rtol, double atol, double delta, int64_t maxiter,
+                        void* ws, int64_t* iters, int64_t* updates, double* rnorm, int32_t* status, cudaStream_t s) {
+  const uint8_t* bc = op.bc;
+  const int64_t n = n_nodes * VEC;
+  const int64_t m = n_values(pat, VEC, FEM_SLICED_DF48);
+  const float* vhi = static_cast<const float*>(vals);
+  const int16_t* vlo = reinterpret_cast<const int16_t*>(static_cast<const char*>(vals) + df_lo_offset(m));
+  KWs w = carve(ws, n, FEM_F64);
+  const size_t f4 = al(sizeof(float) * (size_t)n), d8 = al(sizeof(double) * (size_t)n);
+  char* v = w.vecs;
+  float* xh = reinterpret_cast<float*>(v); v += f4;
+  float* xl = reinterpret_cast<float*>(v); v += f4;
+  float* rh = reinterpret_cast<float*>(v); v += f4;
+  float* rl = reinterpret_cast<float*>(v); v += f4;
+  float* z = reinterpret_cast<float*>(v); v += f4;
+  float2* pp = reinterpret_cast<float2*>(v); v += al(sizeof(float2) * DfNode<VEC>::PAD * (size_t)n_nodes);
+  float* qh = reinterpret_cast<float*>(v); v += f4;
+  float* ql = reinterpret_cast<float*>(v); v += f4;
+  double* ax = reinterpret_cast<double*>(v); v += d8;
+  double* r64 = reinterpret_cast<double*>(v);
+  KCtl* C = w.ctl;
+  const int gv = vec_grid(n), gn = vec_grid(n_nodes);
+  init_ctl_kernel<<<1, 32, 0, s>>>(C, rtol * rtol, atol * atol, (long long)maxiter);
+  dot_kernel<double><<<gv, VTHREADS, 0, s>>>(n, b, b, C, w.partials, nullptr, FIN_REF_BB);
+  f64_to_df_kernel<<<gv, VTHREADS, 0, s>>>(n, x, xh, xl);
+  note_launches(3);
+  int rc = check_launch("pcg_dfx init");
+  if (rc) return rc;
+  // FP64 true residual at the FP64 iterate held in x; r (df) := split(r64)
+  auto true_residual = [&]() -> int {
+    const int r2 = ref_apply<VEC>(pat, n_nodes, op, x, ax, s);
+    if (r2) return r2;
+    refine_residual64_kernel<<<gv, VTHREADS, 0, s>>>(n, b, x, ax, bc, r64, C, w.partials);
+    f64_to_df_kernel<<<gv, VTHREADS, 0, s>>>(n, r64, rh, rl);
+    note_launches(2);
+    return check_launch("refine_residual (df)");
+  };
+  rc = true_residual();
+  if (rc) return rc;
+  KCtl h;
+  rc = poll(C, s, &h);
+  if (rc) return rc;
+  int64_t n_updates = 0;
+  int final_status = FEM_SOLVE_CONVERGED;
+  const double delta2 = delta * delta;
+  if (!(h.rr_true <= h.thresh2)) {
+    FEM_CUDA(cudaMemcpyAsync(&C->delta2, &delta2, sizeof(double), cudaMemcpyHostToDevice, s));
+    pcgx_start_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, rh, rl, z, pp, pc, 1, C, w.partials);
+    note_launches(1);
+    int64_t launched = 0;
+    while (true) {
+      rc = poll(C, s, &h);
+      if (rc) return rc;
+      if (h.done) {
+        if (h.status == SOLVE_UPDATE || h.status == FEM_SOLVE_MAXITER) {
+          const bool at_max = h.status == FEM_SOLVE_MAXITER;
+          df_to_f64_kernel<<<gv, VTHREADS, 0, s>>>(n, xh, xl, x);
+          note_launches(1);
+          rc = true_residual();
+          if (rc) return rc;
+          rc = poll(C, s, &h);
+          if (rc) return rc;
+          ++n_updates;
+          if (h.rr_true <= h.thresh2) { final_status = FEM_SOLVE_CONVERGED; break; }
+          if (!std::isfinite(h.rr_true)) { final_status = FEM_SOLVE_NAN; break; }
+          if (at_max || h.iter >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
+          pcgx_start_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, rh, rl, z, pp, pc, 0, C, w.partials);
+          pcgx_direction_kernel<VEC><<<gn, VTHREADS, 0, s>>>(n_nodes, z, pp, C);
+          note_launches(2);
+          continue;
+        }
+        final_status = h.status;  // NaN or breakdown
+        df_to_f64_kernel<<<gv, VTHREADS, 0, s>>>(n, xh, xl, x);
+        note_launches(1);
+        break;
+      }
+      if (launched >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
+      for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
+        launch_dfdf<VEC>(pat, n_nodes, vhi, vlo, pp, qh, ql, C, FIN_PCG_ALPHA, w.partials, s);
+        pcgx_update_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
+                                                           w.partials, FIN_PCGR_UPDATE);
+        pcgx_direction_kernel<VEC><<<gn, VTHREADS, 0, s>>>(n_nodes, z, pp, C);
+        note_launches(2);
+      }
+      rc = check_launch("pcg_dfx iteration");
+      if (rc) return rc;
+    }
+  }
+  if (iters) *iters = h.iter;
+  if (updates) *updates = n_updates;
+  if (rnorm) *rnorm = std::sqrt(h.rr_true);
+  if (status) *status = final_status;
+  return FEM_OK;
+}
+
+template <int VEC, int PC>
+static int pcg_df_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* vals, const float* pc, const RefOp& op,
                        const double* b, double* x, double rtol, double atol, double delta, int64_t maxiter, void* ws,
-                       int64_t* iters, int64_t* updates, double* rnorm, int32_t* status, cudaStream_t s) {
+                       int64_t* iters, int64_t* updates, double* rnorm, int32_t* status, cudaStream_t s, int mfmt) {
+  const uint8_t* bc = op.bc;
   const int64_t n = n_nodes * VEC;
   const int64_t nnz = pat->nnzb * VEC * VEC;
   const float* vhi = static_cast<const float*>(vals);
-  const int16_t* vlo = reinterpret_cast<const int16_t*>(static_cast<const char*>(vals) + df_lo_offset(nnz));
+  const int64_t m = mfmt == FEM_SLICED_DF48 ? n_values(pat, VEC, mfmt) : nnz;
+  const int16_t* vlo = reinterpret_cast<const int16_t*>(static_cast<const char*>(vals) + df_lo_offset(m));
   KWs w = carve(ws, n, FEM_F64);
   const size_t d8 = al(sizeof(double) * (size_t)n), f4 = al(sizeof(float) * (size_t)n);
   double* r = reinterpret_cast<double*>(w.vecs);
@@ -1029,9 +1746,7 @@ static int pcg_df_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* va
   int rc = check_launch("pcg_df init");
   if (rc) return rc;
   auto true_residual = [&]() -> int {
-    FEM_CUDA(cudaMemsetAsync(ax, 0, sizeof(double) * (size_t)n, s));
-    const int r2 = fem_assemble(mesh, mat, pat, FEM_OUT_APPLY, FEM_F64, u_lin, x, bc, FEM_BC_SYMMETRIC, nullptr,
-                                nullptr, ax, s);
+    const int r2 = ref_apply<VEC>(pat, n_nodes, op, x, ax, s);
     if (r2) return r2;
     refine_residual64_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(n, b, x, ax, bc, r, C, w.partials);
     note_launches(1);
@@ -1076,7 +1791,8 @@ static int pcg_df_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* va
       }
       if (launched >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
       for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
-        launch_spmv_nd<VEC, FMT_DF>(pat, n_nodes, vhi, vlo, phi, plo, q, p, C, FIN_PCG_ALPHA, w.partials, 1, s);
+        launch_spmv_any<VEC, FMT_DF>(pat, n_nodes, mfmt, vhi, vlo, phi, plo, q, p, C, FIN_PCG_ALPHA, w.partials, 1,
+                                     s);
         pcgd_update_kernel<VEC, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, x, r, z, p, q, pc, C, w.partials,
                                                                           FIN_PCGR_UPDATE);
         pcgd_direction_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(n, p, z, phi, plo, C);
@@ -1097,36 +1813,40 @@ static int pcg_df_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* va
 
 using namespace fem;
 
+
 static int check_pat(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision) {
   FEM_REQUIRE(pat && pat->block_ptr && pat->block_cols, "pattern NULL");
   FEM_REQUIRE(n_nodes > 0, "n_nodes must be positive");
   FEM_REQUIRE(vec == 1 || vec == 3, "vec must be 1 or 3");
-  FEM_REQUIRE(precision == FEM_F32 || precision == FEM_F64, "bad precision");
+  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SLICED_DF48, "bad precision");
+  FEM_REQUIRE(!is_sliced(precision) || (pat->n_slices == (n_nodes + 31) / 32 && pat->slice_ptr && pat->slice_cols),
+              "sliced format needs the pattern's slice arrays (fem_pattern_slices)");
   return FEM_OK;
 }
 
 extern "C" int fem_spmv(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision, const void* vals,
                         const void* x, void* y, void* stream) {
-  int rc = check_pat(pat, n_nodes, vec, precision == FEM_DF48 ? FEM_F64 : precision);
+  int rc = check_pat(pat, n_nodes, vec, precision);
   if (rc) return rc;
   FEM_REQUIRE(vals && x && y, "NULL vector");
   cudaStream_t s = as_stream(stream);
-  if (precision == FEM_DF48) {
-    const int64_t n = n_nodes * vec, nnz = pat->nnzb * vec * vec;
+  if (is_df(precision)) {
+    const int64_t n = n_nodes * vec;
     const float* hi = (const float*)vals;
-    const int16_t* lo = reinterpret_cast<const int16_t*>((const char*)vals + df_lo_offset(nnz));
+    const int16_t* lo =
+        reinterpret_cast<const int16_t*>((const char*)vals + df_lo_offset(n_values(pat, vec, precision)));
     const float* xh = (const float*)x;
     const float* xl = xh + n;
-    if (vec == 3) launch_spmv_nd<3, FMT_DF>(pat, n_nodes, hi, lo, xh, xl, y, nullptr, nullptr, 0, nullptr, 0, s);
-    else launch_spmv_nd<1, FMT_DF>(pat, n_nodes, hi, lo, xh, xl, y, nullptr, nullptr, 0, nullptr, 0, s);
+    if (vec == 3) launch_spmv_any<3, FMT_DF>(pat, n_nodes, precision, hi, lo, xh, xl, y, nullptr, nullptr, 0, nullptr, 0, s);
+    else launch_spmv_any<1, FMT_DF>(pat, n_nodes, precision, hi, lo, xh, xl, y, nullptr, nullptr, 0, nullptr, 0, s);
     return check_launch("spmv_df");
   }
-  if (precision == FEM_F32) {
-    if (vec == 3) launch_spmv<3, float>(pat, n_nodes, (const float*)vals, (const float*)x, (float*)y, nullptr, nullptr, 0, nullptr, 0, s);
-    else launch_spmv<1, float>(pat, n_nodes, (const float*)vals, (const float*)x, (float*)y, nullptr, nullptr, 0, nullptr, 0, s);
+  if (vec_f32(precision)) {
+    if (vec == 3) launch_spmv<3, float>(pat, n_nodes, (const float*)vals, (const float*)x, (float*)y, nullptr, nullptr, 0, nullptr, 0, s, precision);
+    else launch_spmv<1, float>(pat, n_nodes, (const float*)vals, (const float*)x, (float*)y, nullptr, nullptr, 0, nullptr, 0, s, precision);
   } else {
-    if (vec == 3) launch_spmv<3, double>(pat, n_nodes, (const double*)vals, (const double*)x, (double*)y, nullptr, nullptr, 0, nullptr, 0, s);
-    else launch_spmv<1, double>(pat, n_nodes, (const double*)vals, (const double*)x, (double*)y, nullptr, nullptr, 0, nullptr, 0, s);
+    if (vec == 3) launch_spmv<3, double>(pat, n_nodes, (const double*)vals, (const double*)x, (double*)y, nullptr, nullptr, 0, nullptr, 0, s, precision);
+    else launch_spmv<1, double>(pat, n_nodes, (const double*)vals, (const double*)x, (double*)y, nullptr, nullptr, 0, nullptr, 0, s, precision);
   }
   return check_launch("spmv");
 }
@@ -1134,6 +1854,7 @@ extern "C" int fem_spmv(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, 
 extern "C" int fem_zero_rows(const fem_pattern_t* pat, int32_t vec, int32_t precision, void* vals, const int32_t* rows,
                              int64_t n_rows, double diag_value, void* stream) {
   FEM_REQUIRE(pat && pat->block_ptr && pat->indptr && pat->diag && vals, "pattern/vals NULL");
+  FEM_REQUIRE(precision == FEM_F32 || precision == FEM_F64, "fem_zero_rows works on CSR-order FP32/FP64 values");
   FEM_REQUIRE(vec == 1 || vec == 3, "vec must be 1 or 3");
   FEM_REQUIRE(n_rows >= 0 && (n_rows == 0 || rows), "rows NULL");
   if (n_rows == 0) return FEM_OK;
@@ -1162,6 +1883,7 @@ extern "C" int fem_precond_setup(const fem_pattern_t* pat, int64_t n_nodes, int3
                                  const void* vals, int32_t pc_kind, void* pc, void* stream) {
   int rc = check_pat(pat, n_nodes, vec, precision);
   if (rc) return rc;
+  FEM_REQUIRE(precision == FEM_F32 || precision == FEM_F64, "preconditioners are set up from CSR FP32/FP64 values");
   FEM_REQUIRE(pc_kind == FEM_PC_JACOBI || pc_kind == FEM_PC_BJACOBI, "pc_kind must be JACOBI or BJACOBI");
   FEM_REQUIRE(vals && pc, "NULL argument");
   cudaStream_t s = as_stream(stream);
@@ -1179,23 +1901,23 @@ extern "C" int fem_precond_setup(const fem_pattern_t* pat, int64_t n_nodes, int3
 
 extern "C" int fem_krylov_workspace(int64_t n_dofs, int32_t precision, size_t* bytes) {
   FEM_REQUIRE(bytes && n_dofs >= 0, "bad arguments");
-  FEM_REQUIRE(precision == FEM_F32 || precision == FEM_F64, "bad precision");
-  *bytes = krylov_ws_bytes(n_dofs, precision);
+  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SLICED_DF48, "bad precision");
+  *bytes = krylov_ws_bytes(n_dofs, vec_f32(precision) ? FEM_F32 : FEM_F64);
   return FEM_OK;
 }
 
 template <typename T>
 static int solve_dispatch(bool bicg, const fem_pattern_t* pat, int64_t n_nodes, int vec, const void* vals, int pc_kind,
                           const void* pc, const void* b, void* x, double rtol, double atol, int64_t maxiter, void* ws,
-                          int64_t* it, double* rn, int32_t* st, cudaStream_t s) {
+                          int64_t* it, double* rn, int32_t* st, cudaStream_t s, int mfmt) {
   const T* V = (const T*)vals;
   const T* P = (const T*)pc;
   const T* B = (const T*)b;
   T* X = (T*)x;
 #define FEM_SOLVE_CASE(VEC, PC)                                                                          \
   if (vec == VEC && pc_kind == PC)                                                                       \
-    return bicg ? bicg_impl<VEC, T, PC>(pat, n_nodes, V, P, B, X, rtol, atol, maxiter, ws, it, rn, st, s) \
-                : pcg_impl<VEC, T, PC>(pat, n_nodes, V, P, B, X, rtol, atol, maxiter, ws, it, rn, st, s);
+    return bicg ? bicg_impl<VEC, T, PC>(pat, n_nodes, V, P, B, X, rtol, atol, maxiter, ws, it, rn, st, s, mfmt) \
+                : pcg_impl<VEC, T, PC>(pat, n_nodes, V, P, B, X, rtol, atol, maxiter, ws, it, rn, st, s, mfmt);
   FEM_SOLVE_CASE(3, FEM_PC_NONE)
   FEM_SOLVE_CASE(3, FEM_PC_JACOBI)
   FEM_SOLVE_CASE(3, FEM_PC_BJACOBI)
@@ -1216,13 +1938,15 @@ static int krylov_entry(bool bicg, const fem_pattern_t* pat, int64_t n_nodes, in
   FEM_REQUIRE(pc_kind == FEM_PC_NONE || pc, "preconditioner data NULL");
   FEM_REQUIRE(pc_kind >= FEM_PC_NONE && pc_kind <= FEM_PC_BJACOBI, "bad pc_kind");
   FEM_REQUIRE(rtol >= 0 && atol >= 0 && maxiter >= 0, "tolerances / maxiter must be non-negative");
-  FEM_REQUIRE(ws_bytes >= krylov_ws_bytes(n_nodes * vec, precision), "krylov workspace too small");
+  FEM_REQUIRE(!is_df(precision), "use fem_pcg_refined for DF48 matrices");
+  FEM_REQUIRE(ws_bytes >= krylov_ws_bytes(n_nodes * vec, vec_f32(precision) ? FEM_F32 : FEM_F64),
+              "krylov workspace too small");
   cudaStream_t s = as_stream(stream);
-  if (precision == FEM_F32)
+  if (vec_f32(precision))
     return solve_dispatch<float>(bicg, pat, n_nodes, vec, vals, pc_kind, pc, b, x, rtol, atol, maxiter, ws, iterations,
-                                 res_norm, status, s);
+                                 res_norm, status, s, precision);
   return solve_dispatch<double>(bicg, pat, n_nodes, vec, vals, pc_kind, pc, b, x, rtol, atol, maxiter, ws, iterations,
-                                res_norm, status, s);
+                                res_norm, status, s, precision);
 }
 
 extern "C" int fem_pcg(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision, const void* vals,
@@ -1274,15 +1998,21 @@ extern "C" int fem_dot(int32_t precision, const void* x, const void* y, int64_t 
 
 extern "C" int fem_pcg_refined(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
                                const void* vals32, int32_t pc_kind, const void* pc32, const fem_mesh_t* mesh,
-                               const fem_material_t* mat, const double* u_lin, const uint8_t* bc_mask,
+                               const fem_material_t* mat, const double* u_lin, const void* vals_ref,
+                               int32_t ref_precision, const uint8_t* bc_mask,
                                const double* b, double* x, double rtol, double atol, double delta, int64_t maxiter,
                                void* ws, size_t ws_bytes, int64_t* iterations, int64_t* updates, double* res_norm,
                                int32_t* status, void* stream) {
-  FEM_REQUIRE(precision == FEM_F32 || precision == FEM_DF48, "precision must be FEM_F32 or FEM_DF48");
-  int rc = check_pat(pat, n_nodes, vec, FEM_F32);
+  FEM_REQUIRE(precision == FEM_F32 || precision == FEM_SLICED_F32 || is_df(precision),
+              "precision must be FEM_F32, FEM_DF48 or a sliced variant");
+  int rc = check_pat(pat, n_nodes, vec, precision);
   if (rc) return rc;
-  FEM_REQUIRE(vals32 && b && x && ws && mesh && mat, "NULL argument");
-  FEM_REQUIRE(mesh->n_nodes == n_nodes && mesh->vec == vec, "mesh does not match the pattern");
+  FEM_REQUIRE(vals32 && b && x && ws, "NULL argument");
+  FEM_REQUIRE(vals_ref || (mesh && mat), "need an FP64 reference matrix or mesh + material");
+  FEM_REQUIRE(!vals_ref || ref_precision == FEM_F64 || ref_precision == FEM_SLICED_F64,
+              "reference matrix must be FEM_F64 or FEM_SLICED_F64");
+  FEM_REQUIRE(vals_ref || (mesh->n_nodes == n_nodes && mesh->vec == vec), "mesh does not match the pattern");
+  const RefOp op{mesh, mat, u_lin, vals_ref, ref_precision, bc_mask};
   FEM_REQUIRE(pc_kind == FEM_PC_NONE || pc32, "preconditioner data NULL");
   FEM_REQUIRE(pc_kind >= FEM_PC_NONE && pc_kind <= FEM_PC_BJACOBI, "bad pc_kind");
   FEM_REQUIRE(rtol >= 0 && atol >= 0 && maxiter >= 0 && delta > 0 && delta < 1, "bad tolerances");
@@ -1292,11 +2022,14 @@ extern "C" int fem_pcg_refined(const fem_pattern_t* pat, int64_t n_nodes, int32_
   const float* P = (const float*)pc32;
 #define FEM_REF_CASE(VEC, PC)                                                                                   \
   if (vec == VEC && pc_kind == PC)                                                                              \
-    return precision == FEM_DF48                                                                                \
-               ? pcg_df_impl<VEC, PC>(pat, n_nodes, vals32, P, mesh, mat, u_lin, bc_mask, b, x, rtol, atol, delta, \
-                                      maxiter, ws, iterations, updates, res_norm, status, s)                   \
-               : pcg_refined_impl<VEC, PC>(pat, n_nodes, V, P, mesh, mat, u_lin, bc_mask, b, x, rtol, atol, delta, \
-                                           maxiter, ws, iterations, updates, res_norm, status, s);
+    return precision == FEM_SLICED_DF48                                                                         \
+               ? pcg_dfx_impl<VEC, PC>(pat, n_nodes, vals32, P, op, b, x, rtol, atol, delta, maxiter, ws,       \
+                                       iterations, updates, res_norm, status, s)                               \
+           : is_df(precision)                                                                                   \
+               ? pcg_df_impl<VEC, PC>(pat, n_nodes, vals32, P, op, b, x, rtol, atol, delta, maxiter, ws,        \
+                                      iterations, updates, res_norm, status, s, precision)                     \
+               : pcg_refined_impl<VEC, PC>(pat, n_nodes, V, P, op, b, x, rtol, atol, delta, maxiter, ws,        \
+                                           iterations, updates, res_norm, status, s, precision);
   FEM_REF_CASE(3, FEM_PC_NONE)
   FEM_REF_CASE(3, FEM_PC_JACOBI)
   FEM_REF_CASE(3, FEM_PC_BJACOBI)
@@ -1307,23 +2040,51 @@ extern "C" int fem_pcg_refined(const fem_pattern_t* pat, int64_t n_nodes, int32_
   return fail(FEM_ERR_ARG, "bad vec / preconditioner");
 }
 
-extern "C" int fem_matrix_bytes(int64_t nnz, int32_t precision, size_t* bytes) {
-  FEM_REQUIRE(bytes && nnz >= 0, "bad arguments");
-  if (precision == FEM_F32) *bytes = sizeof(float) * (size_t)nnz;
-  else if (precision == FEM_F64) *bytes = sizeof(double) * (size_t)nnz;
-  else if (precision == FEM_DF48) *bytes = df_lo_offset(nnz) + sizeof(int16_t) * (size_t)nnz;
-  else return fail(FEM_ERR_ARG, "bad precision");
+extern "C" int fem_matrix_bytes(const fem_pattern_t* pat, int32_t vec, int32_t precision, size_t* bytes) {
+  FEM_REQUIRE(pat && bytes && (vec == 1 || vec == 3), "bad arguments");
+  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SLICED_DF48, "bad precision");
+  FEM_REQUIRE(!is_sliced(precision) || pat->n_slices > 0, "sliced format needs fem_pattern_slices first");
+  const int64_t m = n_values(pat, vec, precision);
+  if (is_df(precision)) *bytes = df_lo_offset(m) + sizeof(int16_t) * (size_t)m;
+  else if (vec_f32(precision)) *bytes = sizeof(float) * (size_t)m;
+  else *bytes = sizeof(double) * (size_t)m;
   return FEM_OK;
 }
 
-extern "C" int fem_matrix_split(const double* vals64, int64_t nnz, void* vals_df, void* stream) {
-  FEM_REQUIRE(nnz >= 0 && (nnz == 0 || (vals64 && vals_df)), "NULL argument");
-  if (nnz == 0) return FEM_OK;
-  float* hi = (float*)vals_df;
-  int16_t* lo = reinterpret_cast<int16_t*>((char*)vals_df + df_lo_offset(nnz));
-  split_df_kernel<<<grid_for(nnz, 256), 256, 0, as_stream(stream)>>>(vals64, nnz, hi, lo);
+extern "C" int fem_matrix_convert(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, const double* vals64,
+                                  int32_t precision, void* out, void* stream) {
+  int rc = check_pat(pat, n_nodes, vec, precision);
+  if (rc) return rc;
+  FEM_REQUIRE(vals64 && out, "NULL argument");
+  FEM_REQUIRE(precision != FEM_F64, "FP64 CSR values need no conversion");
+  cudaStream_t s = as_stream(stream);
+  const int64_t nnz = pat->nnzb * vec * vec;
+  if (precision == FEM_DF48) {
+    float* hi = (float*)out;
+    int16_t* lo = reinterpret_cast<int16_t*>((char*)out + df_lo_offset(nnz));
+    split_df_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(vals64, nnz, hi, lo);
+  } else if (precision == FEM_F32) {
+    cast_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(vals64, (float*)out, nnz, nullptr);
+  } else {
+    const int64_t m = n_values(pat, vec, precision);
+    int16_t* lo = is_df(precision) ? reinterpret_cast<int16_t*>((char*)out + df_lo_offset(m)) : nullptr;
+    const int g = grid_for(pat->n_slices * 32, 256);
+#define FEM_TO_SLICED(VEC, OUT)                                                                              \
+  to_sliced_kernel<VEC, OUT><<<g, 256, 0, s>>>(n_nodes, pat->n_slices, pat->block_ptr, pat->slice_ptr, vals64, \
+                                                out, lo)
+    if (vec == 3) {
+      if (precision == FEM_SLICED_F64) FEM_TO_SLICED(3, FEM_SLICED_F64);
+      else if (precision == FEM_SLICED_F32) FEM_TO_SLICED(3, FEM_SLICED_F32);
+      else FEM_TO_SLICED(3, FEM_SLICED_DF48);
+    } else {
+      if (precision == FEM_SLICED_F64) FEM_TO_SLICED(1, FEM_SLICED_F64);
+      else if (precision == FEM_SLICED_F32) FEM_TO_SLICED(1, FEM_SLICED_F32);
+      else FEM_TO_SLICED(1, FEM_SLICED_DF48);
+    }
+#undef FEM_TO_SLICED
+  }
   note_launches(1);
-  return check_launch("split_df");
+  return check_launch("matrix_convert");
 }
 
 extern "C" int fem_vector_split(const double* x, int64_t n, float* x_df, void* stream) {
@@ -1332,6 +2093,29 @@ extern "C" int fem_vector_split(const double* x, int64_t n, float* x_df, void* s
   split_vec_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(x, n, x_df, x_df + n);
   note_launches(1);
   return check_launch("split_vec");
+}
+
+extern "C" int fem_spmv_dfx(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, const void* vals,
+                            const void* x_df, float* y_hi, float* y_lo, double* xy_dot, void* ws, size_t ws_bytes,
+                            void* stream) {
+  FEM_REQUIRE(pat && vals && x_df && y_hi && y_lo && ws, "NULL argument");
+  FEM_REQUIRE(vec == 1 || vec == 3, "vec must be 1 or 3");
+  FEM_REQUIRE(pat->n_slices > 0 && pat->slice_ptr && pat->slice_cols, "pattern has no sliced layout");
+  FEM_REQUIRE(ws_bytes >= krylov_ws_bytes(n_nodes * vec, FEM_F64), "workspace too small");
+  cudaStream_t s = as_stream(stream);
+  const int64_t m = n_values(pat, vec, FEM_SLICED_DF48);
+  const float* vhi = static_cast<const float*>(vals);
+  const int16_t* vlo = reinterpret_cast<const int16_t*>(static_cast<const char*>(vals) + df_lo_offset(m));
+  KWs w = carve(ws, n_nodes * vec, FEM_F64);
+  init_ctl_kernel<<<1, 32, 0, s>>>(w.ctl, 0.0, 0.0, 0);
+  note_launches(1);
+  const float2* xp = static_cast<const float2*>(x_df);
+  if (vec == 3) launch_dfdf<3>(pat, n_nodes, vhi, vlo, xp, y_hi, y_lo, w.ctl, FIN_DOT, w.partials, s);
+  else launch_dfdf<1>(pat, n_nodes, vhi, vlo, xp, y_hi, y_lo, w.ctl, FIN_DOT, w.partials, s);
+  int rc = check_launch("spmv_dfx");
+  if (rc) return rc;
+  if (xy_dot) FEM_CUDA(cudaMemcpyAsync(xy_dot, &w.ctl->d0, sizeof(double), cudaMemcpyDeviceToDevice, s));
+  return FEM_OK;
 }
 
 // ---- allocation-free PCG ----------------------------------------------------------
@@ -1386,15 +2170,16 @@ extern "C" int fem_pcg_static(const fem_pattern_t* pat, int64_t n_nodes, int32_t
   FEM_REQUIRE(pc_kind == FEM_PC_NONE || pc, "preconditioner data NULL");
   FEM_REQUIRE(pc_kind >= FEM_PC_NONE && pc_kind <= FEM_PC_BJACOBI, "bad pc_kind");
   FEM_REQUIRE(rtol >= 0 && atol >= 0 && maxiter >= 0, "tolerances / maxiter must be non-negative");
+  FEM_REQUIRE(!is_df(precision), "fem_pcg_static takes FP32 / FP64 (CSR or sliced) matrices");
   void* ws = nullptr;
   rc = static_pcg_scratch(&ws);
   if (rc) return rc;
   // the control block (done flag, tickets, scalars) is reset by the solver's first kernel;
   // partial sums and vectors are written before they are read, so nothing else is cleared
   cudaStream_t s = as_stream(stream);
-  if (precision == FEM_F32)
+  if (vec_f32(precision))
     return solve_dispatch<float>(false, pat, n_nodes, vec, vals, pc_kind, pc, b, x, rtol, atol, maxiter, ws,
-                                 iterations, res_norm, status, s);
+                                 iterations, res_norm, status, s, precision);
   return solve_dispatch<double>(false, pat, n_nodes, vec, vals, pc_kind, pc, b, x, rtol, atol, maxiter, ws,
-                                iterations, res_norm, status, s);
+                                iterations, res_norm, status, s, precision);
 }

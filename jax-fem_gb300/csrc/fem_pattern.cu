@@ -316,3 +316,53 @@ extern "C" int fem_pattern_scalar(int64_t n_nodes, int32_t vec, const int64_t* b
   if (rc) return rc;
   return read_err(err, s, "fem_pattern_scalar");
 }
+
+// ---- sliced layout: 32 node rows per slice, width = longest row in the slice --------
+namespace fem {
+__global__ void slice_width_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* bp, int64_t* widths) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n_slices; s += (int64_t)gridDim.x * blockDim.x) {
+    int64_t w = 0;
+    for (int l = 0; l < 32; ++l) {
+      const int64_t i = s * 32 + l;
+      if (i < n_nodes) { const int64_t nb = bp[i + 1] - bp[i]; w = nb > w ? nb : w; }
+    }
+    widths[s] = w;
+  }
+}
+
+// slice_cols[(slice_ptr[s] + k) * 32 + l] = block column k of node 32 s + l (0 beyond the row)
+__global__ void slice_cols_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* bp, const int32_t* bcols,
+                                  const int64_t* sp, int32_t* scols) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_slices * 32; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = t >> 5;
+    const int l = (int)(t & 31);
+    const int64_t i = s * 32 + l;
+    const int64_t b0 = i < n_nodes ? bp[i] : 0;
+    const int64_t nb = i < n_nodes ? bp[i + 1] - b0 : 0;
+    for (int64_t k = 0; k < sp[s + 1] - sp[s]; ++k)
+      scols[(sp[s] + k) * 32 + l] = k < nb ? bcols[b0 + k] : 0;
+  }
+}
+}  // namespace fem
+
+extern "C" int fem_pattern_slices(int64_t n_nodes, const int64_t* block_ptr, const int32_t* block_cols,
+                                  int64_t* slice_ptr, int32_t* slice_cols, int64_t* n_slots, void* stream) {
+  FEM_REQUIRE(n_nodes > 0 && block_ptr && block_cols && slice_ptr, "bad arguments");
+  cudaStream_t s = as_stream(stream);
+  const int64_t n_slices = (n_nodes + 31) / 32;
+  if (slice_cols == nullptr) {
+    FEM_REQUIRE(n_slots, "n_slots NULL");
+    slice_width_kernel<<<grid_for(n_slices, 256), 256, 0, s>>>(n_nodes, n_slices, block_ptr, slice_ptr);
+    scan_single_block<<<1, SCAN_THREADS, 0, s>>>(slice_ptr, n_slices);
+    note_launches(2);
+    int rc = check_launch("slice widths");
+    if (rc) return rc;
+    FEM_CUDA(cudaMemcpyAsync(n_slots, slice_ptr + n_slices, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    FEM_CUDA(cudaStreamSynchronize(s));
+    return FEM_OK;
+  }
+  slice_cols_kernel<<<grid_for(n_slices * 32, 256), 256, 0, s>>>(n_nodes, n_slices, block_ptr, block_cols, slice_ptr,
+                                                                  slice_cols);
+  note_launches(1);
+  return check_launch("slice cols");
+}

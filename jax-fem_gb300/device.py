@@ -50,7 +50,7 @@ class DeviceCSR:
         return self.eng.scalar_indices()
 
     def matvec(self, x):
-        if self.precision == _lib.FEM_DF48:
+        if self.precision in (_lib.FEM_DF48, _lib.FEM_SLICED_DF48):
             x = x.to(torch.float64).contiguous()
             xs = torch.empty(2 * x.numel(), dtype=torch.float32, device=x.device)
             call("fem_vector_split", ptr(x), x.numel(), ptr(xs), _stream())
@@ -58,13 +58,17 @@ class DeviceCSR:
             call("fem_spmv", C.byref(self.eng.pattern), self.eng.num_nodes, self.eng.vec, self.precision,
                  ptr(self.data), ptr(xs), ptr(y), _stream())
             return y
-        x = x.to(self.data.dtype).contiguous()
+        x = x.to(self.vector_dtype).contiguous()
         y = torch.empty_like(x)
         call("fem_spmv", C.byref(self.eng.pattern), self.eng.num_nodes, self.eng.vec, self.precision,
              ptr(self.data), ptr(x), ptr(y), _stream())
         return y
 
     __matmul__ = matvec
+
+    @property
+    def vector_dtype(self):
+        return torch.float32 if self.precision in (_lib.FEM_F32, _lib.FEM_SLICED_F32) else torch.float64
 
     def diagonal(self):
         if self.source is not None:
@@ -75,9 +79,13 @@ class DeviceCSR:
         if kind == _lib.FEM_PC_NONE:
             return None
         if self.source is not None:
-            # FP32 preconditioner of a DF48 matrix, set up from its FP64 source values
+            # preconditioner of a derived (sliced / DF48) matrix, set up from its FP64 CSR source;
+            # FP64 for FP64 solver copies, FP32 otherwise
             if kind not in self.pc:
                 pc64 = self.source.preconditioner(kind)
+                if self.precision == _lib.FEM_SLICED_F64:
+                    self.pc[kind] = pc64
+                    return pc64
                 pc = torch.empty(pc64.numel(), dtype=torch.float32, device=pc64.device)
                 call("fem_cast_f64_f32", ptr(pc64), ptr(pc), pc64.numel(), None, _stream())
                 self.pc[kind] = pc
@@ -159,8 +167,20 @@ class Engine:
         call("fem_pattern_scalar", self.num_nodes, self.vec, ptr(self.block_ptr), ptr(self.block_cols),
              ptr(self.indptr), ptr(self.diag), None, s)
         self.nnz = self.nnzb * self.vec * self.vec
+        # sliced layout (32 node rows per slice) of the solver copies of the matrix
+        self.n_slices = (self.num_nodes + 31) // 32
+        self.slice_ptr = torch.empty(self.n_slices + 1, dtype=torch.int64, device=dev)
+        n_slots = C.c_int64()
+        call("fem_pattern_slices", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols), ptr(self.slice_ptr),
+             None, C.byref(n_slots), s)
+        self.n_slots = n_slots.value
+        self.slice_cols = torch.empty(self.n_slots * 32, dtype=torch.int32, device=dev)
+        call("fem_pattern_slices", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols), ptr(self.slice_ptr),
+             ptr(self.slice_cols), None, s)
         self.pattern = _lib.FemPattern(self.nnzb, self.block_ptr.data_ptr(), self.block_cols.data_ptr(),
-                                       self.indptr.data_ptr(), self.diag.data_ptr(), self.slots.data_ptr())
+                                       self.indptr.data_ptr(), self.diag.data_ptr(), self.slots.data_ptr(),
+                                       self.n_slices, self.n_slots, self.slice_ptr.data_ptr(),
+                                       self.slice_cols.data_ptr())
         self._indices = None
 
     def scalar_indices(self):
@@ -286,17 +306,21 @@ class Engine:
         key = (precision, bc_mode)
         if cache and m.linear and key in self._tangent_cache:
             return self._tangent_cache[key]
-        if precision == _lib.FEM_DF48:
+        if precision not in (_lib.FEM_F32, _lib.FEM_F64):
+            # solver copies (DF48, sliced FP32 / FP64 / DF48) are converted from the FP64 CSR tangent
             A64 = self.tangent(dofs, _lib.FEM_F64, bc_mode, cache=cache)
             nb = C.c_size_t()
-            call("fem_matrix_bytes", self.nnz, _lib.FEM_DF48, C.byref(nb))
-            buf = getattr(self, f"valsdf_{bc_mode}", None)
+            call("fem_matrix_bytes", C.byref(self.pattern), self.vec, precision, C.byref(nb))
+            name = f"valsx{precision}_{bc_mode}"
+            buf = getattr(self, name, None)
             if buf is None or buf.numel() != nb.value:
                 buf = torch.empty(nb.value, dtype=torch.uint8, device=self.device)
-                setattr(self, f"valsdf_{bc_mode}", buf)
-            t0 = time.perf_counter()
-            call("fem_matrix_split", ptr(A64.data), self.nnz, ptr(buf), _stream())
-            A = DeviceCSR(self, _lib.FEM_DF48, buf, bc_mode, source=A64)
+                setattr(self, name, buf)
+            call("fem_matrix_convert", C.byref(self.pattern), self.num_nodes, self.vec, ptr(A64.data), precision,
+                 ptr(buf), _stream())
+            view = buf.view(torch.float64) if precision == _lib.FEM_SLICED_F64 else \
+                buf.view(torch.float32) if precision == _lib.FEM_SLICED_F32 else buf
+            A = DeviceCSR(self, precision, view, bc_mode, source=A64)
             self._tangent_cache[key] = A
             return A
         dtype = torch.float32 if precision == _lib.FEM_F32 else torch.float64
@@ -355,14 +379,14 @@ class Engine:
 
     def krylov(self, method, A, b, x, pc_kind, rtol, atol, maxiter):
         """Run fem_pcg / fem_bicgstab; x is updated in place. Returns (iterations, residual norm, status)."""
-        ws = self.workspace(A.precision)
+        ws = self.workspace(_lib.FEM_F32 if A.vector_dtype == torch.float32 else _lib.FEM_F64)
         pc = A.preconditioner(pc_kind)
         it, rn, st = C.c_int64(), C.c_double(), C.c_int32()
         t0 = time.perf_counter()
         call("fem_pcg" if method == "cg" else "fem_bicgstab", C.byref(self.pattern), self.num_nodes, self.vec,
              A.precision, ptr(A.data), pc_kind, ptr(pc), ptr(b), ptr(x), float(rtol), float(atol), int(maxiter),
              ptr(ws), ws.numel(), C.byref(it), C.byref(rn), C.byref(st), _stream())
-        rec = dict(method=method, precision="fp32" if A.precision == _lib.FEM_F32 else "fp64",
+        rec = dict(method=method, precision={0: "fp32", 1: "fp64", 3: "sliced-fp32", 4: "sliced-fp64"}.get(A.precision),
                    iterations=it.value, res_norm=rn.value, status=_lib.SOLVE_STATUS.get(st.value, "?"),
                    seconds=time.perf_counter() - t0)
         self.solve_log.append(rec)
@@ -379,12 +403,15 @@ class Engine:
         pc = A32.preconditioner(pc_kind)
         it, up, rn, st = C.c_int64(), C.c_int64(), C.c_double(), C.c_int32()
         t0 = time.perf_counter()
+        ref = A32.source if A32.source is not None and A32.source.bc_mode == _lib.FEM_BC_SYMMETRIC else None
         call("fem_pcg_refined", C.byref(self.pattern), self.num_nodes, self.vec, A32.precision, ptr(A32.data),
              pc_kind, ptr(pc),
-             C.byref(self.mesh), C.byref(ms), ptr(u_lin.contiguous()), ptr(self.bc_mask), ptr(b.contiguous()), ptr(x),
+             C.byref(self.mesh), C.byref(ms), ptr(u_lin.contiguous()), None if ref is None else ptr(ref.data),
+             _lib.FEM_F64 if ref is None else ref.precision, ptr(self.bc_mask), ptr(b.contiguous()), ptr(x),
              float(rtol), float(atol), float(delta), int(maxiter), ptr(ws), ws.numel(), C.byref(it), C.byref(up),
              C.byref(rn), C.byref(st), _stream())
-        rec = dict(method="cg-refined", precision="df48+fp64" if A32.precision == _lib.FEM_DF48 else "fp32+fp64",
+        rec = dict(method="cg-refined",
+                   precision="df48+fp64" if A32.precision in (_lib.FEM_DF48, _lib.FEM_SLICED_DF48) else "fp32+fp64",
                    iterations=it.value, updates=up.value,
                    res_norm=rn.value, status=_lib.SOLVE_STATUS.get(st.value, "?"), seconds=time.perf_counter() - t0)
         self.solve_log.append(rec)

@@ -108,7 +108,11 @@ def _precision(cfg):
 
 
 def _mixed_matrix_precision(precision):
-    return _lib.FEM_DF48 if precision == "mixed" else _lib.FEM_F32
+    """Solver copy of the tangent: sliced DF48 for 'mixed', sliced FP32 for 'mixed32'."""
+    return _lib.FEM_SLICED_DF48 if precision == "mixed" else _lib.FEM_SLICED_F32
+
+
+_FP64_SOLVER_FORMAT = _lib.FEM_SLICED_F64     # FP64 Krylov iterations run on the sliced FP64 copy
 
 
 def get_A(problem):
@@ -127,8 +131,10 @@ def linear_solver(A, b, x0, linear_options, precision="fp64", inner_rtol=1e-5):
     eng = A.eng
     if spec.custom is not None:
         return spec.custom(A, b, x0, linear_options)
+    if A.precision in (_lib.FEM_DF48, _lib.FEM_SLICED_DF48):
+        raise NotImplementedError("DF48 matrices are solved by the mixed Newton / adjoint paths (fem_pcg_refined)")
     x = torch.zeros_like(b) if x0 is None else x0.clone()
-    if A.precision == _lib.FEM_F64:
+    if A.vector_dtype == torch.float64:
         it, rn, st = eng.krylov(spec.method, A, b.contiguous(), x, spec.pc, spec.rtol, spec.atol, spec.maxiter)
         return x, (it, rn, st)
     b32 = eng.cast32(b)
@@ -146,9 +152,9 @@ def _timed(eng, key, t0):
 def _newton_step(problem, eng, dofs, res, spec, precision, cfg):
     """One Newton correction A inc = -res (solver.py:390-421) with the Dirichlet rows of the
     increment equal to g - u_b."""
-    prec = _lib.FEM_F64 if precision == "fp64" else _mixed_matrix_precision(precision)
-    if prec == _lib.FEM_DF48 and spec.method != "cg":
-        prec = _lib.FEM_F32          # BiCGStab mixed path runs in FP32 with Newton-level refinement
+    prec = _FP64_SOLVER_FORMAT if precision == "fp64" else _mixed_matrix_precision(precision)
+    if prec == _lib.FEM_SLICED_DF48 and spec.method != "cg":
+        prec = _lib.FEM_SLICED_F32   # BiCGStab mixed path runs in FP32 with Newton-level refinement
     eng.refresh_bc()
     rows = eng.bc_rows_long
     du_b = eng.bc_vals - dofs[rows] if eng.n_bc else None
@@ -173,7 +179,7 @@ def _newton_step(problem, eng, dofs, res, spec, precision, cfg):
             b = b - eng.apply(dofs, x0, skip_bc_rows=True)
         b[rows] = du_b
     inner = cfg.get("inner_rtol", 1e-5)
-    if prec == _lib.FEM_F64:
+    if prec == _FP64_SOLVER_FORMAT:
         x = x0.clone()
         it, rn, st = eng.krylov(spec.method, A, b, x, spec.pc, spec.rtol, spec.atol, spec.maxiter)
         if spec.method == "bicgstab":
@@ -206,7 +212,7 @@ def _newton_step(problem, eng, dofs, res, spec, precision, cfg):
             new[rows] = eng.bc_vals      # constraints hold exactly in FP64
         return new
     new = dofs + inc
-    if prec != _lib.FEM_F64 and eng.n_bc:
+    if prec != _FP64_SOLVER_FORMAT and eng.n_bc:
         new[rows] = eng.bc_vals
     return new
 
@@ -306,12 +312,12 @@ def adjoint_solve(problem, dofs, v, adjoint_solver_options=None, precision="fp64
         return torch.as_tensor(spec.custom(A, b, None, spec.options), dtype=torch.float64, device=dofs.device)
     t0 = time.perf_counter()
     if prec_opt == "fp64":
-        A = eng.tangent(dofs, _lib.FEM_F64, _lib.FEM_BC_SYMMETRIC)
+        A = eng.tangent(dofs, _FP64_SOLVER_FORMAT, _lib.FEM_BC_SYMMETRIC)
         lam = torch.zeros_like(b)
         eng.krylov(spec.method, A, b, lam, spec.pc, spec.rtol, spec.atol, spec.maxiter)
         _timed(eng, "linear", t0)
         return lam
-    mprec = _mixed_matrix_precision(prec_opt) if spec.method == "cg" else _lib.FEM_F32
+    mprec = _mixed_matrix_precision(prec_opt) if spec.method == "cg" else _lib.FEM_SLICED_F32
     A = eng.tangent(dofs, mprec, _lib.FEM_BC_SYMMETRIC)
     lam = torch.zeros_like(b)
     if spec.method == "cg":

@@ -353,11 +353,14 @@ def test_df48_spmv_matches_fp64(cuda):
     eng = prob._engine
     z = torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda)
     A64 = eng.tangent(z, jf._lib.FEM_F64, jf._lib.FEM_BC_SYMMETRIC, cache=False)
-    Adf = eng.tangent(z, jf._lib.FEM_DF48, jf._lib.FEM_BC_SYMMETRIC, cache=False)
     x = torch.randn(eng.num_dofs, dtype=torch.float64, device=cuda)
     y64 = A64.matvec(x)
-    ydf = Adf.matvec(x)
-    assert (ydf - y64).abs().max().item() <= 1e-11 * y64.abs().max().item()
+    L = jf._lib
+    for fmt, tol in ((L.FEM_DF48, 1e-11), (L.FEM_SLICED_DF48, 1e-11), (L.FEM_SLICED_F64, 1e-14),
+                     (L.FEM_SLICED_F32, 1e-6)):
+        A = eng.tangent(z, fmt, jf._lib.FEM_BC_SYMMETRIC, cache=False)
+        y = A.matvec(x).double()
+        assert (y - y64).abs().max().item() <= tol * y64.abs().max().item(), fmt
 
 
 def test_mixed32_variant_converges(cuda):
@@ -369,3 +372,48 @@ def test_mixed32_variant_converges(cuda):
     s32, J32, g32 = _simp_grad(prob, theta_np, cuda, dict(o, precision="mixed32"), dict(o, precision="mixed32"))
     assert (s32 - s64).abs().max().item() <= 1e-8 * s64.abs().max().item()
     assert np.abs(g32 - g64).max() <= 1e-7 * np.abs(g64).max()
+
+
+def _df_nodes(x, vec):
+    """Node-interleaved double-float copy of an FP64 vector (the fem_spmv_dfx input layout)."""
+    pad = 4 if vec == 3 else 1
+    hi = x.float()
+    lo = (x - hi.double()).float()
+    xp = torch.zeros(x.numel() // vec, pad, 2, dtype=torch.float32, device=x.device)
+    xp[:, :vec, 0] = hi.view(-1, vec)
+    xp[:, :vec, 1] = lo.view(-1, vec)
+    return xp
+
+
+@pytest.mark.parametrize("n", [(10, 5, 3), (64, 40, 40)])
+def test_spmv_dfx_matches_fp64(cuda, n):
+    """The mixed CG's SpMV (bulk-copy staged, double-float in and out) against the FP64 SpMV:
+    y to 1e-11 of max|y|, the fused dot x.y to 1e-11 relative.  (64, 40, 40) has more slices
+    than resident warps, so warps stream several slices through their shared-memory ring."""
+    import ctypes as C
+    import jax_fem_gb300 as jf
+    import cases
+    L = jf._lib
+    prob, _, theta_np = cases.simp_box(*n)
+    prob.set_params(torch.tensor(theta_np, device=cuda))
+    eng = prob._engine
+    z = torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda)
+    A64 = eng.tangent(z, L.FEM_F64, L.FEM_BC_SYMMETRIC, cache=False)
+    Adf = eng.tangent(z, L.FEM_SLICED_DF48, L.FEM_BC_SYMMETRIC, cache=False)
+    g = torch.Generator(device=cuda).manual_seed(3)
+    x = torch.randn(eng.num_dofs, dtype=torch.float64, device=cuda, generator=g)
+    y64 = A64.matvec(x)
+    xp = _df_nodes(x, 3)
+    yh = torch.empty(eng.num_dofs, dtype=torch.float32, device=cuda)
+    yl = torch.empty_like(yh)
+    dot = torch.zeros(1, dtype=torch.float64, device=cuda)
+    nb = C.c_size_t()
+    L.call("fem_krylov_workspace", eng.num_dofs, L.FEM_SLICED_DF48, C.byref(nb))
+    ws = torch.empty(nb.value, dtype=torch.uint8, device=cuda)
+    for _ in range(2):  # a second call reuses the workspace and its control block
+        L.call("fem_spmv_dfx", C.byref(eng.pattern), eng.num_nodes, 3, L.ptr(Adf.data), L.ptr(xp), L.ptr(yh),
+               L.ptr(yl), L.ptr(dot), L.ptr(ws), nb.value, L.stream_handle())
+        y = yh.double() + yl.double()
+        assert (y - y64).abs().max().item() <= 1e-11 * y64.abs().max().item()
+        ref = torch.dot(x, y64).item()
+        assert abs(dot.item() - ref) <= 1e-11 * abs(ref)
