@@ -206,6 +206,15 @@ __device__ __forceinline__ float df_lo_scale(float hi) {
   return e > 39 ? __int_as_float((e - 39) << 23) : 0.0f;   // 2^(e - 166) = ulp(hi) / 2^16
 }
 
+// DF48 correction without an int->float conversion: base is the float 1.5 * 2^(E-143) (E the
+// exponent field of hi); adding q (|q| < 2^15) to its mantissa field gives (1.5 + q/2^23) *
+// 2^(E-143), and subtracting base leaves exactly q * 2^(E-166) = q * ulp(hi) / 2^16.  Encoders
+// write q = 0 whenever E <= 39, where base may wrap: the result is then 0 as required.
+__device__ __forceinline__ float df48_lo(float hi, int q) {
+  const int base = (__float_as_int(hi) & 0x7f800000) + (0x400000 - (16 << 23));
+  return __int_as_float(base + q) - __int_as_float(base);
+}
+
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& err) {
   s = a + b;
   const float bb = s - a;
@@ -505,8 +514,7 @@ spmv_sliced_dfdf_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* __rest
       for (int v = 0; v < VV; ++v) {
         const int r = v / VEC, d = v % VEC;
         const float ah = __ldcs(vals + vb + v * 32);
-        const float sc = __int_as_float((__float_as_int(ah) & 0x7f800000) - (39 << 23));
-        const float al = (float)__ldcs(vlo + vb + v * 32) * sc;
+        const float al = df48_lo(ah, __ldcs(vlo + vb + v * 32));
         df_acc(sh[r], sl[r], df2{ah, al}, df2{xvh[d], xvl[d]});
       }
     }
@@ -663,8 +671,7 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
           for (int v = 0; v < VV; ++v) {
             const int r = v / VEC, d = v % VEC;
             const float ah = sv[(t * VV + v) * 32 + lane];
-            const float sc2 = __int_as_float((__float_as_int(ah) & 0x7f800000) - (39 << 23));
-            const float al = (float)sq[(t * VV + v) * 32 + lane] * sc2;
+            const float al = df48_lo(ah, sq[(t * VV + v) * 32 + lane]);
             df_acc(sh[r], sl[r], df2{ah, al}, df2{xvh[t][d], xvl[t][d]});
           }
         }
@@ -1034,6 +1041,107 @@ __global__ void pcgx_update_kernel(int64_t n_nodes, float* xh, float* xl, float*
   reduce_and_finalize<2>(dv, C, op, partials, C->ticket + 1, nullptr);
 }
 
+// vec-3 form of pcgx_update_kernel with every global access coalesced: a warp takes a tile of
+// 32 nodes (96 dofs); the dof-ordered arrays (x, r, q, z) move in three full lines per array,
+// the preconditioner blocks in nine, and the node-wise z = M r.h regroups through shared memory
+// (strides 3 and 9 are bank-conflict free).
+constexpr int VTILE_WARPS = VTHREADS / 32;
+template <int PC>
+__global__ void __launch_bounds__(VTHREADS)
+pcgx_update_tile_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restrict__ xl, float* __restrict__ rh,
+                        float* __restrict__ rl, float* __restrict__ z, const float2* __restrict__ pp,
+                        const float* __restrict__ qh, const float* __restrict__ ql, const float* __restrict__ pc,
+                        KCtl* C, double* partials, int op) {
+  constexpr int PCW = PC == FEM_PC_BJACOBI ? 9 : PC == FEM_PC_JACOBI ? 3 : 0;
+  __shared__ float s_r[VTILE_WARPS][96], s_rl[VTILE_WARPS][96], s_z[VTILE_WARPS][96];
+  __shared__ float s_pc[VTILE_WARPS][PCW > 0 ? 32 * PCW : 1];
+  if (C->done) return;
+  const df2 a = df_of(C->alpha);
+  const df2 na{-a.h, -a.l};
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  float* sr = s_r[w];
+  float* srl = s_rl[w];
+  float* sz = s_z[w];
+  float* spc = s_pc[w];
+  float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f;
+  const int64_t ntiles = (n_nodes + 31) / 32;
+  const int64_t nw = (int64_t)gridDim.x * VTILE_WARPS;
+  for (int64_t t = (int64_t)blockIdx.x * VTILE_WARPS + w; t < ntiles; t += nw) {
+    const int64_t node0 = t * 32;
+    const int nn = n_nodes - node0 < 32 ? (int)(n_nodes - node0) : 32;
+    const int nd = 3 * nn;
+    const int64_t d0 = 3 * node0;
+#pragma unroll
+    for (int j = 0; j < PCW; ++j) {
+      const int o = 32 * j + lane;
+      if (o < PCW * nn) spc[o] = pc[PCW * node0 + o];
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int o = 32 * j + lane;
+      if (o < nd) {
+        const int64_t k = d0 + o;
+        const int nl = o / 3, c = o - 3 * nl;
+        const float2 pv = pp[(node0 + nl) * 4 + c];
+        const df2 x = df_add(df2{xh[k], xl[k]}, df_mul(a, df2{pv.x, pv.y}));
+        xh[k] = x.h;
+        xl[k] = x.l;
+        const df2 r = df_add(df2{rh[k], rl[k]}, df_mul(na, df2{qh[k], ql[k]}));
+        rh[k] = r.h;
+        rl[k] = r.l;
+        sr[o] = r.h;
+        srl[o] = r.l;
+      }
+    }
+    __syncwarp();
+    if (lane < nn) {
+      float rv[3] = {sr[3 * lane], sr[3 * lane + 1], sr[3 * lane + 2]};
+      float zv[3];
+      if constexpr (PC == FEM_PC_BJACOBI) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          zv[c] = spc[9 * lane + 3 * c] * rv[0] + spc[9 * lane + 3 * c + 1] * rv[1] + spc[9 * lane + 3 * c + 2] * rv[2];
+      } else if constexpr (PC == FEM_PC_JACOBI) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) zv[c] = spc[3 * lane + c] * rv[c];
+      } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) zv[c] = rv[c];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        sz[3 * lane + c] = zv[c];
+        const df2 r{rv[c], srl[3 * lane + c]};
+        df_acc(s0, e0, r, df2{zv[c], 0.f});
+        df_acc(s1, e1, r, r);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int o = 32 * j + lane;
+      if (o < nd) z[d0 + o] = sz[o];
+    }
+    __syncwarp();
+  }
+  double dv[3] = {(double)s0 + (double)e0, (double)s1 + (double)e1, 0.0};
+  reduce_and_finalize<2>(dv, C, op, partials, C->ticket + 1, nullptr);
+}
+
+// vec-3 form of pcgx_direction_kernel, thread per dof: z coalesced, p gathered within the tile.
+__global__ void pcgx_direction3_kernel(int64_t n, const float* __restrict__ z, float2* __restrict__ pp,
+                                       const KCtl* C) {
+  if (C->done) return;
+  const df2 b = df_of(C->beta);
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = k / 3;
+    const int64_t o = i * 4 + (k - 3 * i);
+    const float2 pv = pp[o];
+    const df2 p = df_add(df2{z[k], 0.f}, df_mul(b, df2{pv.x, pv.y}));
+    pp[o] = make_float2(p.h, p.l);
+  }
+}
+
 // p = z + beta p (df), the SpMV input of the next iteration
 template <int VEC>
 __global__ void pcgx_direction_kernel(int64_t n_nodes, const float* z, float2* pp, const KCtl* C) {
@@ -1267,7 +1375,7 @@ static KWs carve(void* ws, int64_t n_dofs, int precision) {
 }
 
 static int vec_grid(int64_t n) {
-  int g = grid_for(n, VTHREADS, 4);
+  int g = grid_for(n, VTHREADS, 8);
   return g > MAX_PARTIAL_BLOCKS ? MAX_PARTIAL_BLOCKS : g;
 }
 
@@ -1647,6 +1755,16 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
   double* r64 = reinterpret_cast<double*>(v);
   KCtl* C = w.ctl;
   const int gv = vec_grid(n), gn = vec_grid(n_nodes);
+  // tile kernel: one warp per 32-node tile, grid = resident CTAs (no partial second wave)
+  static int tile_per_sm = 0;
+  if (tile_per_sm == 0 &&
+      (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tile_per_sm, pcgx_update_tile_kernel<PC>, VTHREADS, 0) !=
+           cudaSuccess ||
+       tile_per_sm < 1))
+    tile_per_sm = 1;
+  int gt = (int)std::min<int64_t>((int64_t)sm_count() * tile_per_sm, ((n_nodes + 31) / 32 + VTILE_WARPS - 1) / VTILE_WARPS);
+  if (gt > MAX_PARTIAL_BLOCKS) gt = MAX_PARTIAL_BLOCKS;
+  if (gt < 1) gt = 1;
   init_ctl_kernel<<<1, 32, 0, s>>>(C, rtol * rtol, atol * atol, (long long)maxiter);
   dot_kernel<double><<<gv, VTHREADS, 0, s>>>(n, b, b, C, w.partials, nullptr, FIN_REF_BB);
   f64_to_df_kernel<<<gv, VTHREADS, 0, s>>>(n, x, xh, xl);
@@ -1704,9 +1822,15 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
       if (launched >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
       for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
         launch_dfdf<VEC>(pat, n_nodes, vhi, vlo, pp, qh, ql, C, FIN_PCG_ALPHA, w.partials, s);
-        pcgx_update_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
-                                                           w.partials, FIN_PCGR_UPDATE);
-        pcgx_direction_kernel<VEC><<<gn, VTHREADS, 0, s>>>(n_nodes, z, pp, C);
+        if constexpr (VEC == 3) {
+          pcgx_update_tile_kernel<PC><<<gt, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
+                                                              w.partials, FIN_PCGR_UPDATE);
+          pcgx_direction3_kernel<<<gv, VTHREADS, 0, s>>>(n, z, pp, C);
+        } else {
+          pcgx_update_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
+                                                             w.partials, FIN_PCGR_UPDATE);
+          pcgx_direction_kernel<VEC><<<gn, VTHREADS, 0, s>>>(n_nodes, z, pp, C);
+        }
         note_launches(2);
       }
       rc = check_launch("pcg_dfx iteration");
