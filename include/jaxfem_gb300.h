@@ -189,6 +189,19 @@ int fem_param_vjp(const fem_mesh_t* mesh, const fem_material_t* mat, const doubl
 int fem_j2_update(const fem_mesh_t* mesh, const fem_material_t* mat, const double* u,
                   double* history_out, void* stream);
 
+/* Reverse mode of the J2 material through its history, for gradients over several load steps
+ * (the reference takes jax.grad over a loop of fwd_pred and update_int_vars_gp:
+ * applications/crystal_plasticity/volume_sensitivity.py:89-107; return map and update
+ * test_plasticity.py:54-78).  Exactly one of:
+ *   lam (adjoint mode): cotangents of -lam^T R(u; history, scale) (lam masked on Dirichlet dofs);
+ *   hist_bar (update mode, (cells, nq, 18)): cotangents of fem_j2_update's outputs
+ *     (sigma_new 9 | eps_new 9); u_grad (n_dofs, accumulated: +=) receives the cotangent of u.
+ * hist_grad (cells, nq, 18) receives the cotangents of the input history (sigma_old | eps_old);
+ * scale_grad (cells, nq), optional, those of the modulus-scale field. */
+int fem_j2_history_vjp(const fem_mesh_t* mesh, const fem_material_t* mat, const double* u, const double* lam,
+                       const uint8_t* bc_mask, const double* hist_bar, double* hist_grad, double* scale_grad,
+                       double* u_grad, void* stream);
+
 /* ---- Dirichlet rows -------------------------------------------------------
  * fem_zero_rows: PETSc zeroRows with KEEP_NONZERO_PATTERN (solver.py:477,527-528):
  *   every entry of each listed row := 0, then the diagonal := diag_value.

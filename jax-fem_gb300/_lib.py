@@ -75,6 +75,7 @@ SIGNATURES = {
     "fem_assemble": ([PMESH, PMAT, PPAT, I32, I32, P, P, P, I32, P, P, P, P], C.c_int),
     "fem_param_vjp": ([PMESH, PMAT, P, P, P, P, P], C.c_int),
     "fem_j2_update": ([PMESH, PMAT, P, P, P], C.c_int),
+    "fem_j2_history_vjp": ([PMESH, PMAT, P, P, P, P, P, P, P, P], C.c_int),
     "fem_zero_rows": ([PPAT, I32, I32, P, P, I64, F64, P], C.c_int),
     "fem_apply_bc_vec": ([P, P, P, P, I64, F64, P], C.c_int),
     "fem_spmv": ([PPAT, I64, I32, I32, P, P, P, P], C.c_int),

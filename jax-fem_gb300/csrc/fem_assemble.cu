@@ -358,3 +358,27 @@ extern "C" int fem_j2_update(const fem_mesh_t* mesh, const fem_material_t* mat, 
   P.hist_out = history_out;
   return run_cell_kernel(mesh, P, mat->kind, FEM_F64, KMODE_HIST, as_stream(stream));
 }
+
+extern "C" int fem_j2_history_vjp(const fem_mesh_t* mesh, const fem_material_t* mat, const double* u,
+                                  const double* lam, const uint8_t* bc_mask, const double* hist_bar,
+                                  double* hist_grad, double* scale_grad, double* u_grad, void* stream) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  FEM_REQUIRE(mat && mat->kind == FEM_MAT_J2 && mesh->vec == 3, "history VJP needs a J2 material on vec=3");
+  FEM_REQUIRE(u && hist_grad, "NULL argument");
+  FEM_REQUIRE((lam == nullptr) != (hist_bar == nullptr), "give exactly one of lam (adjoint) and hist_bar (update)");
+  FEM_REQUIRE(!(lam && u_grad), "u_grad is only produced in update mode (hist_bar)");
+  FEM_REQUIRE(!scale_grad || (mat->n_qp_params == 1 && mat->qp_params), "scale_grad needs the modulus-scale field");
+  if (mesh->n_cells == 0) return FEM_OK;
+  AsmParams P;
+  rc = fill_params(mesh, mat, P);
+  if (rc) return rc;
+  P.u = u;
+  P.w = lam;
+  P.bc = lam ? bc_mask : nullptr;
+  P.hist_bar = hist_bar;
+  P.hist_out = hist_grad;
+  P.vjp_out = scale_grad;
+  P.res = u_grad;
+  return run_cell_kernel(mesh, P, mat->kind, FEM_F64, KMODE_HVJP, as_stream(stream));
+}

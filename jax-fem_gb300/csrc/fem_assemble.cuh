@@ -41,10 +41,11 @@ struct AsmParams {
   void* vals;
   double* apply_out;
   double* vjp_out;        // fem_param_vjp
-  double* hist_out;       // fem_j2_update
+  double* hist_out;       // fem_j2_update; fem_j2_history_vjp: history cotangent (C, Q, 18)
+  const double* hist_bar; // fem_j2_history_vjp update mode: cotangents of (sigma_new, eps_new)
 };
 
-enum { KMODE_ASSEMBLE = 0, KMODE_VJP = 1, KMODE_HIST = 2 };
+enum { KMODE_ASSEMBLE = 0, KMODE_VJP = 1, KMODE_HIST = 2, KMODE_HVJP = 3 };
 
 template <int NN, int VEC>
 struct Cpb {
@@ -101,7 +102,9 @@ cell_kernel(const AsmParams P) {
   const bool want_res = (KMODE == KMODE_ASSEMBLE) && (P.outputs & FEM_OUT_RESIDUAL);
   const bool want_mat = (KMODE == KMODE_ASSEMBLE) && (P.outputs & FEM_OUT_MATRIX);
   const bool want_app = (KMODE == KMODE_ASSEMBLE) && (P.outputs & FEM_OUT_APPLY);
-  const bool need_w = want_app || KMODE == KMODE_VJP;
+  const bool need_w = want_app || KMODE == KMODE_VJP || (KMODE == KMODE_HVJP && P.w != nullptr);
+  // history VJP in update mode scatters the cotangent of u (residual-style) into P.res
+  const bool want_ubar = (KMODE == KMODE_HVJP) && (P.res != nullptr);
 
   const int64_t n_tiles = (P.n_cells + CPB - 1) / CPB;
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
@@ -122,7 +125,8 @@ cell_kernel(const AsmParams P) {
           if (need_w) {
             T wv = T(P.w[dof]);
             // VJP: multiplier masked on Dirichlet dofs; APPLY with FEM_BC_SYMMETRIC: K_ff w_f
-            if (P.bc && P.bc[dof] && (KMODE == KMODE_VJP || P.bc_mode == FEM_BC_SYMMETRIC)) wv = T(0);
+            if (P.bc && P.bc[dof] && (KMODE == KMODE_VJP || KMODE == KMODE_HVJP || P.bc_mode == FEM_BC_SYMMETRIC))
+              wv = T(0);
             sW[k * VEC + v] = wv;
           }
         }
@@ -176,6 +180,27 @@ cell_kernel(const AsmParams P) {
         P.vjp_out[(e * NQ + q) * P.n_qp] = -double(acc) * double(jxw);
         continue;
       }
+      if constexpr (KMODE == KMODE_HVJP) {
+        if constexpr (MAT == FEM_MAT_J2 && VEC == 3) {
+          T gs[9], ge[9];
+          if (P.w) {  // adjoint mode: cotangent of sigma is -jxw grad(lambda)
+            for (int s = 0; s < 9; ++s) { gs[s] = -gw[s] * jxw; ge[s] = T(0); }
+          } else {
+            const double* hb = P.hist_bar + (e * NQ + q) * 18;
+            for (int s = 0; s < 9; ++s) { gs[s] = T(hb[s]); ge[s] = T(hb[9 + s]); }
+          }
+          T W[9], dso[9], deo[9], dsc;
+          Mat::hist_vjp(gu, P.mc, qp, hs, gs, ge, W, dso, deo, dsc);
+          double* ho = P.hist_out + (e * NQ + q) * 18;
+          for (int s = 0; s < 9; ++s) { ho[s] = double(dso[s]); ho[9 + s] = double(deo[s]); }
+          if (P.vjp_out) P.vjp_out[e * NQ + q] = double(dsc);
+          if (want_ubar) {
+            T* Sq = sS + (c * NQ + q) * NS;
+            for (int s = 0; s < 9; ++s) Sq[s] = W[s];
+          }
+        }
+        continue;
+      }
       if constexpr (KMODE == KMODE_HIST) {
         if constexpr (VEC == 3) {
           T S[NS];
@@ -213,7 +238,8 @@ cell_kernel(const AsmParams P) {
       if (want_mat)
         for (int s = 0; s < NTAN; ++s) tq[s] *= jxw;
     }
-    if constexpr (KMODE != KMODE_ASSEMBLE) continue;
+    if constexpr (KMODE != KMODE_ASSEMBLE && KMODE != KMODE_HVJP) continue;
+    if (KMODE == KMODE_HVJP && !want_ubar) continue;
     __syncthreads();
     // ---- C / D: element rows ---------------------------------------------
     const int c = tid / (NN * VEC);
@@ -278,7 +304,7 @@ cell_kernel(const AsmParams P) {
       }
     }
 
-    if (want_res || want_app) {
+    if (want_res || want_app || want_ubar) {
       double rv = 0.0;
       if (active) {
         T s = T(0);
@@ -300,7 +326,7 @@ cell_kernel(const AsmParams P) {
       if (emit && lane == __ffs(grp) - 1) {
         double sum = 0.0;
         for (unsigned m = grp; m; m &= m - 1) sum += sRed[(tid & ~31) + __ffs(m) - 1];
-        atomicAdd(want_res ? (P.res + row) : (P.apply_out + row), sum);
+        atomicAdd((want_res || want_ubar) ? (P.res + row) : (P.apply_out + row), sum);
       }
       __syncwarp();
     }
@@ -330,6 +356,10 @@ template <int NN, int NQ, int VEC, int MAT>
 int dispatch_precision(const AsmParams& P, int precision, int kmode, cudaStream_t s) {
   if (kmode == KMODE_VJP) return launch_cell_kernel<NN, NQ, VEC, MAT, double, KMODE_VJP>(P, s);
   if (kmode == KMODE_HIST) return launch_cell_kernel<NN, NQ, VEC, MAT, double, KMODE_HIST>(P, s);
+  if (kmode == KMODE_HVJP) {
+    if constexpr (MAT == FEM_MAT_J2 && VEC == 3) return launch_cell_kernel<NN, NQ, VEC, MAT, double, KMODE_HVJP>(P, s);
+    return fail(FEM_ERR_UNSUPPORTED, "history VJP is defined for J2 only");
+  }
   if (precision == FEM_F32) return launch_cell_kernel<NN, NQ, VEC, MAT, float, KMODE_ASSEMBLE>(P, s);
   return launch_cell_kernel<NN, NQ, VEC, MAT, double, KMODE_ASSEMBLE>(P, s);
 }

@@ -259,6 +259,45 @@ struct Material<FEM_MAT_J2, 3, T> {
       dS[k] = dtr[k] - beta * T(2) * mu0 * dev - gam * sde * st.s[k];
     }
   }
+  // Reverse mode through the return map and the history update (test_plasticity.py:54-78).
+  // Given cotangents gs of sigma_new (9) and ge of eps_new = sym(g) (9), returns the cotangent W
+  // of g = grad u (9), of sigma_old (dso), eps_old (deo) and of the E scale (dsc).
+  // sigma depends on sigma_tr only, with D = d sigma / d sigma_tr
+  //   = (1 - beta) I + (beta / 3) I(x)I - (3 sig0 / (2 q^3)) s(x)s   (identity when elastic),
+  // and sigma_tr = C : (sym(g) - eps_old) + sigma_old.
+  __device__ static void hist_vjp(const T g[9], const MatConsts& mc, const double* qp, const double* hist,
+                                  const T gs[9], const T ge[9], T W[9], T dso[9], T deo[9], T& dsc) {
+    State st;
+    trial(g, mc, qp, hist, st);
+    T z[9];
+    if (st.plastic) {
+      const T sig0 = T(mc.c[2]);
+      const T beta = T(1) - sig0 / st.q;
+      const T c3 = T(1.5) * sig0 / (st.q * st.q * st.q);
+      const T trg = gs[0] + gs[4] + gs[8];
+      T gss = T(0);
+      for (int k = 0; k < 9; ++k) gss += gs[k] * st.s[k];
+      for (int k = 0; k < 9; ++k)
+        z[k] = (T(1) - beta) * gs[k] + ((k == 0 || k == 4 || k == 8) ? beta * trg / T(3) : T(0)) - c3 * gss * st.s[k];
+    } else {
+      for (int k = 0; k < 9; ++k) z[k] = gs[k];
+    }
+    // y = C^T : z on the 9 components of deps (deps_ij = sym(g)_ij - eps_old_ij)
+    const T trz = z[0] + z[4] + z[8];
+    T y[9];
+    for (int k = 0; k < 9; ++k) y[k] = T(2) * st.mu * z[k] + ((k == 0 || k == 4 || k == 8) ? st.lam * trz : T(0));
+    for (int k = 0; k < 9; ++k) {
+      dso[k] = z[k];
+      deo[k] = -y[k];
+    }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        W[i * 3 + j] = T(0.5) * (y[i * 3 + j] + y[j * 3 + i]) + T(0.5) * (ge[i * 3 + j] + ge[j * 3 + i]);
+    T dS[9];
+    dparam(g, mc, qp, hist, dS);
+    dsc = T(0);
+    for (int k = 0; k < 9; ++k) dsc += gs[k] * dS[k];
+  }
 };
 
 }  // namespace fem

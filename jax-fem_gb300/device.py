@@ -361,6 +361,21 @@ class Engine:
              ptr(self.bc_mask), ptr(g), _stream())
         return g
 
+    def j2_history_vjp(self, dofs, lam=None, hist_bar=None, want_scale=False, want_u=False):
+        """fem_j2_history_vjp: cotangents of the J2 history (cells, nq, 18) and of the modulus scale
+        (cells*nq, or None); in update mode (hist_bar) also that of u (n_dofs, or None)."""
+        self.refresh_bc()
+        m, ms = self.material()
+        nq = self.num_cells * self.num_quads
+        hg = torch.empty(nq * 18, dtype=torch.float64, device=self.device)
+        sg = torch.empty(nq, dtype=torch.float64, device=self.device) if want_scale else None
+        ug = torch.zeros(self.num_dofs, dtype=torch.float64, device=self.device) if want_u else None
+        hb = None if hist_bar is None else hist_bar.to(torch.float64).reshape(-1).contiguous()
+        call("fem_j2_history_vjp", C.byref(self.mesh), C.byref(ms), ptr(dofs.contiguous()),
+             None if lam is None else ptr(lam.contiguous()), ptr(self.bc_mask), None if hb is None else ptr(hb),
+             ptr(hg), ptr(sg), ptr(ug), _stream())
+        return hg.reshape(self.num_cells, self.num_quads, 18), sg, ug
+
     def j2_update(self, dofs):
         m, ms = self.material()
         out = torch.empty(self.num_cells * self.num_quads * 18, dtype=torch.float64, device=self.device)

@@ -39,6 +39,10 @@ class Material:
         """Return (qp_params tensor or None, history tensor or None) on the device (FP64, contiguous)."""
         return None, None
 
+    def diff_vars(self):
+        """Differentiable internal variables: [(index into internal_vars, 'qp' | 'sigma' | 'eps')]."""
+        return [] if self.param_index is None else [(self.param_index, "qp")]
+
 
 def _per_qp(t, num_cells, num_quads, device, name):
     t = torch.as_tensor(t, dtype=torch.float64, device=device)
@@ -143,6 +147,10 @@ class J2Plasticity(Material):
 
     def consts(self):
         return [self.E, self.nu, self.sig0]
+
+    def diff_vars(self):
+        # the history (sigmas_old, epsilons_old) is differentiable too: gradients over load steps
+        return [(0, "sigma"), (1, "eps")] + ([(2, "qp")] if self.modulus_field else [])
 
     def bind(self, internal_vars, num_cells, num_quads, device):
         if len(internal_vars) < 2:

@@ -347,63 +347,153 @@ def adjoint_solve(problem, dofs, v, adjoint_solver_options=None, precision="fp64
     return lam
 
 
+def _iv_cotangent(iv, g, eng, what):
+    """Reshape a per-point cotangent g to the internal variable iv's shape."""
+    if iv.numel() == g.numel():
+        return g.reshape(iv.shape)
+    if what == "qp" and iv.numel() == eng.num_cells:
+        return g.reshape(eng.num_cells, eng.num_quads).sum(1).reshape(iv.shape)
+    raise ValueError(f"unexpected shape {tuple(iv.shape)} of a differentiable internal variable ({what})")
+
+
 def implicit_vjp(problem, sol_list, params, v_list, adjoint_solver_options, precision="fp64"):
-    """solver.py:1362-1418: returns -lam^T dc/dp with c = apply_bc(R(u, set_params(p)))."""
+    """solver.py:1362-1418: returns -lam^T dc/dp with c = apply_bc(R(u, set_params(p))).
+
+    params is a tensor or a list/tuple of tensors (the reference's params pytree); the result has
+    the same structure.  The cotangent reaches params through set_params by torch autograd, from
+    every differentiable internal variable of the material (per-point parameters; for J2 also the
+    history sigmas_old / epsilons_old, so gradients chain over load steps)."""
     eng = problem._engine
     t0 = time.perf_counter()
+    seq = isinstance(params, (list, tuple))
+    plist = list(params) if seq else [params]
     with torch.no_grad():
-        problem.set_params(params.detach())
+        problem.set_params([p.detach() for p in plist] if seq else params.detach())
         dofs = _flat_v(sol_list, eng.device)
         v = _flat_v(v_list, eng.device)
         lam = adjoint_solve(problem, dofs, v, adjoint_solver_options, precision)
-        g_qp = eng.param_vjp(dofs, lam)
-    m = eng._mat
+        m = eng._mat
+        dv = m.diff_vars()
+        cot = {}
+        if m.history:
+            kinds = {k for _, k in dv}
+            hg, sg, _ = eng.j2_history_vjp(dofs, lam=lam, want_scale="qp" in kinds)
+            cot["sigma"] = hg[:, :, :9]
+            cot["eps"] = hg[:, :, 9:]
+            if sg is not None:
+                cot["qp"] = sg
+        elif dv:
+            cot["qp"] = eng.param_vjp(dofs, lam)
     with torch.enable_grad():
-        p = params.detach().clone().requires_grad_(True)
-        problem.set_params(p)
-        iv = problem.internal_vars[m.param_index]
-        if not (torch.is_tensor(iv) and iv.requires_grad):
+        ps = [p.detach().clone().requires_grad_(True) if torch.is_tensor(p) and p.is_floating_point() else p
+              for p in plist]
+        problem.set_params(ps if seq else ps[0])
+        ivs, gos = [], []
+        for idx, what in dv:
+            iv = problem.internal_vars[idx] if idx < len(problem.internal_vars) else None
+            if torch.is_tensor(iv) and iv.requires_grad:
+                ivs.append(iv)
+                gos.append(_iv_cotangent(iv, cot[what], eng, what).to(iv.dtype))
+        if not ivs:
             raise RuntimeError("set_params must build internal_vars from params with torch operations so the "
                                "parameter chain rule can be applied")
-        if iv.numel() == g_qp.numel():
-            go = g_qp.reshape(iv.shape)
-        elif iv.numel() == eng.num_cells:
-            go = g_qp.reshape(eng.num_cells, eng.num_quads).sum(1).reshape(iv.shape)
-        else:
-            raise ValueError("unexpected internal variable shape for the parameter VJP")
-        (g,) = torch.autograd.grad(iv, p, grad_outputs=go.to(iv.dtype), allow_unused=True)
+        diff_ps = [p for p in ps if torch.is_tensor(p) and p.requires_grad]
+        gs = torch.autograd.grad(ivs, diff_ps, grad_outputs=gos, allow_unused=True)
     with torch.no_grad():
-        problem.set_params(params.detach())
+        problem.set_params([p.detach() for p in plist] if seq else params.detach())
     eng.timing["adjoint"] += time.perf_counter() - t0
-    if g is None:
-        g = torch.zeros_like(params)
-    return g.to(params.dtype)
+    it = iter(gs)
+    out = []
+    for p, q in zip(plist, ps):
+        if torch.is_tensor(q) and q.requires_grad:
+            g = next(it)
+            out.append(torch.zeros_like(p) if g is None else g.to(p.dtype))
+        else:
+            out.append(None)
+    return out if seq else out[0]
 
 
 def ad_wrapper(problem, solver_options={}, adjoint_solver_options={}):
-    """solver.py:1421-1455: differentiable fwd_pred(params) -> sol_list (torch.autograd)."""
+    """solver.py:1421-1455: differentiable fwd_pred(params) -> sol_list (torch.autograd).
+    params may be a tensor or a list/tuple of tensors."""
     _, cfg = _resolve_solver_options(solver_options)
     precision = _precision(cfg)
 
     class _ForwardPrediction(torch.autograd.Function):
         @staticmethod
-        def forward(ctx, params):
-            problem.set_params(params.detach())
+        def forward(ctx, seq, *params):
+            problem.set_params(list(params) if seq else params[0])
             sol_list = solver(problem, solver_options)
-            ctx.save_for_backward(params)
+            ctx.save_for_backward(*params)
+            ctx.seq = seq
             ctx.sol_list = [s.detach() for s in sol_list]
             return tuple(sol_list)
 
         @staticmethod
         def backward(ctx, *v):
-            (params,) = ctx.saved_tensors
+            params = ctx.saved_tensors
             logger.info("Running backward and solving the adjoint problem...")
-            return implicit_vjp(problem, ctx.sol_list, params, list(v), adjoint_solver_options, precision)
+            p = list(params) if ctx.seq else params[0]
+            g = implicit_vjp(problem, ctx.sol_list, p, list(v), adjoint_solver_options, precision)
+            return (None,) + (tuple(g) if ctx.seq else (g,))
 
     def fwd_pred(params):
-        return list(_ForwardPrediction.apply(params))
+        if isinstance(params, (list, tuple)):
+            return list(_ForwardPrediction.apply(True, *params))
+        return list(_ForwardPrediction.apply(False, params))
 
     return fwd_pred
+
+
+class _J2HistoryUpdate(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, problem, sol, sigmas_old, epsilons_old, scale):
+        eng = problem._engine
+        saved = problem.internal_vars
+        ivs = [sigmas_old.detach(), epsilons_old.detach()] + ([] if scale is None else [scale.detach()])
+        problem.internal_vars = ivs
+        try:
+            dofs = sol.detach().reshape(-1).to(torch.float64).contiguous()
+            sig, eps = eng.j2_update(dofs)
+        finally:
+            problem.internal_vars = saved
+        ctx.problem = problem
+        ctx.has_scale = scale is not None
+        ctx.save_for_backward(sol, sigmas_old, epsilons_old, *( [] if scale is None else [scale]))
+        return sig.reshape(sigmas_old.shape), eps.reshape(epsilons_old.shape)
+
+    @staticmethod
+    def backward(ctx, g_sig, g_eps):
+        problem = ctx.problem
+        eng = problem._engine
+        sol, sigmas_old, epsilons_old = ctx.saved_tensors[:3]
+        scale = ctx.saved_tensors[3] if ctx.has_scale else None
+        nc, nq = eng.num_cells, eng.num_quads
+        gz = lambda g: torch.zeros(nc, nq, 9, dtype=torch.float64, device=eng.device) if g is None \
+            else g.reshape(nc, nq, 9).to(torch.float64)
+        hbar = torch.cat([gz(g_sig), gz(g_eps)], dim=2)
+        saved = problem.internal_vars
+        problem.internal_vars = [sigmas_old.detach(), epsilons_old.detach()] + \
+            ([] if scale is None else [scale.detach()])
+        try:
+            dofs = sol.detach().reshape(-1).to(torch.float64).contiguous()
+            hg, sg, ug = eng.j2_history_vjp(dofs, hist_bar=hbar, want_scale=scale is not None, want_u=True)
+        finally:
+            problem.internal_vars = saved
+        g_scale = None
+        if scale is not None:
+            g_scale = _iv_cotangent(scale, sg, eng, "qp").to(scale.dtype)
+        return (None, ug.reshape(sol.shape).to(sol.dtype), hg[:, :, :9].reshape(sigmas_old.shape),
+                hg[:, :, 9:].reshape(epsilons_old.shape), g_scale)
+
+
+def update_j2_history(problem, sol, sigmas_old, epsilons_old, scale=None):
+    """Differentiable J2 history update (test_plasticity.py:73-78, the reference's
+    update_stress_strain / update_int_vars_gp): returns (sigmas_new, epsilons_new) of shape
+    (num_cells, num_quads, 3, 3) for the displacement sol, given the previous history and the
+    optional modulus-scale field.  Its backward is fem_j2_history_vjp in update mode, so
+    torch.autograd chains gradients across load steps."""
+    return _J2HistoryUpdate.apply(problem, sol, sigmas_old, epsilons_old, scale)
 
 
 # ---- BC helpers of the reference, device versions (solver.py:290-363) ----------------
