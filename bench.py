@@ -302,6 +302,39 @@ def bench_reference(args):
     print(json.dumps(line))
 
 
+def kernel_shares(args):
+    """Per-kernel device time of one warm TO step in each precision, from a CUPTI activity trace
+    (torch.profiler): launches, total, share and time per launch.  A profile, not a bench line."""
+    import collections
+    import torch
+    import jax_fem_gb300 as jf
+    from torch.profiler import profile, ProfilerActivity
+    n = tuple(args.size)
+    prob = make_problem(n)
+    th0 = theta_init(prob.num_cells).cuda()
+    with profile(activities=[ProfilerActivity.CUDA]):
+        torch.ones(8, device="cuda").sum().item()     # CUPTI start-up outside the traced step
+    for prec in ("mixed", "fp64"):
+        fwd_o, adj_o = options(prec)
+        fwd = jf.ad_wrapper(prob, fwd_o, adj_o)
+        run_steps(prob, fwd, theta_step(th0, 0))
+        torch.cuda.synchronize()
+        with profile(activities=[ProfilerActivity.CUDA]) as p:
+            run_steps(prob, fwd, theta_step(th0, 1))
+            torch.cuda.synchronize()
+        tot, cnt = collections.defaultdict(float), collections.Counter()
+        for e in p.events():
+            if e.device_type == torch.autograd.DeviceType.CUDA:
+                k = e.name.split("(")[0]
+                tot[k] += getattr(e, "device_time_total", 0.0) or e.cuda_time_total
+                cnt[k] += 1
+        T = sum(tot.values())
+        print(f"{prec} step, {workload_name(n)[0]}: {T / 1e3:.1f} ms of kernel time, {sum(cnt.values())} launches")
+        print(f"{'launches':>9} {'total_ms':>10} {'share':>7} {'us/launch':>10}  kernel")
+        for k, v in sorted(tot.items(), key=lambda kv: -kv[1])[:16]:
+            print(f"{cnt[k]:9d} {v / 1e3:10.2f} {100 * v / T:6.2f}% {v / cnt[k]:10.2f}  {k}")
+
+
 def _default_iters(n):
     # Jacobi-PCG iterations grow ~linearly with the longest mesh dimension for this cantilever
     return (int(12 * max(n)), int(12 * max(n)))
@@ -316,7 +349,12 @@ def main():
     ap.add_argument("--size", type=int, nargs=3, default=list(DEFAULT_SIZE))
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--kernel-shares", action="store_true",
+                    help="print per-kernel device time of one step per precision (CUPTI trace) and exit")
     args = ap.parse_args()
+    if args.kernel_shares:
+        kernel_shares(args)
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
