@@ -297,6 +297,30 @@ int fem_axpy_f32_f64(double alpha, const float* x, double* y, int64_t n, void* s
 int fem_dot(int32_t precision, const void* x, const void* y, int64_t n, double* out,
             void* ws, size_t ws_bytes, void* stream);
 
+/* ---- topology-optimisation update (jax_fem/mma.py) ------------------------------------ */
+/* Workspace bytes of fem_mma_update for n design variables and m constraints (1 <= m <= 4). */
+int fem_mma_workspace(int64_t n, int32_t m, size_t* bytes);
+/* One MMA update (MMA.mmasub, mma.py:113-206, with subsolv, mma.py:209-405), all per-variable
+ * work on the GPU.  Device arrays (n): xval, xold1, xold2, xmin, xmax, df0dx; dfdx (m x n,
+ * row-major); low / upp are read (iter > 2) and written; xmma receives the new design.  Host
+ * arrays (m): fval, a, c, d.  iter is the reference's epoch (asymptotes re-initialised while
+ * iter <= 2).  newton_steps (host, optional) receives the interior-point Newton step count. */
+int fem_mma_update(int64_t n, int32_t m, int32_t iter, const double* xval, const double* xold1,
+                   const double* xold2, double* low, double* upp, const double* xmin, const double* xmax,
+                   double move, const double* df0dx, const double* fval, const double* dfdx, double a0,
+                   const double* a, const double* c, const double* d, double* xmma, void* ws, size_t ws_bytes,
+                   int32_t* newton_steps, void* stream);
+/* Filter of compute_filter_kd_tree (mma.py:27-57): for each of n centroids (device, n x 3) the
+ * at most nnb nearest centroids closer than rmin, weights rmin - distance, stored nnb per row
+ * (cols = -1 in unused slots), hs = row sums.  Ties at the nnb-th distance keep lower indices. */
+int fem_filter_workspace(int64_t n, size_t* bytes);
+int fem_filter_build(int64_t n, const double* centroids, double rmin, int32_t nnb, int32_t* cols, double* vals,
+                     double* hs, void* ws, size_t ws_bytes, void* stream);
+/* mode 0: applySensitivityFilter (mma.py:59-62) on nr rows g (nr x n): H (rho g / max(1e-3, rho) / Hs);
+ * mode 1: applyDensityFilter (mma.py:64-66): H g / Hs. */
+int fem_filter_apply(int64_t n, int32_t nnb, const int32_t* cols, const double* vals, const double* hs,
+                     const double* rho, const double* g, int32_t nr, int32_t mode, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -94,6 +94,12 @@ SIGNATURES = {
     "fem_cast_f64_f32": ([P, P, I64, P, P], C.c_int),
     "fem_axpy_f32_f64": ([F64, P, P, I64, P], C.c_int),
     "fem_dot": ([I32, P, P, I64, P, P, SZ, P], C.c_int),
+    "fem_mma_workspace": ([I64, I32, PSZ], C.c_int),
+    "fem_mma_update": ([I64, I32, I32, P, P, P, P, P, P, P, F64, P, PF64, P, F64, PF64, PF64, PF64, P, P, SZ, PI32, P],
+                       C.c_int),
+    "fem_filter_workspace": ([I64, PSZ], C.c_int),
+    "fem_filter_build": ([I64, P, F64, I32, P, P, P, P, SZ, P], C.c_int),
+    "fem_filter_apply": ([I64, I32, P, P, P, P, P, I32, I32, P, P], C.c_int),
 }
 
 _lib = None
