@@ -335,6 +335,83 @@ def kernel_shares(args):
             print(f"{cnt[k]:9d} {v / 1e3:10.2f} {100 * v / T:6.2f}% {v / cnt[k]:10.2f}  {k}")
 
 
+def mma_update_bench(args):
+    """TO update beside the step (jax_fem/mma.py): sensitivity filter + one MMA update for every
+    cell of the workload as design variable (m = 1 volume constraint), GPU against the oracle's
+    numpy/scipy restatement on the host.  Prints one JSON line; not the headline metric."""
+    import torch
+    import jax_fem_gb300 as jf
+    import importlib
+    M = importlib.import_module("jax_fem_gb300.mma")
+    n = tuple(args.size)
+    name, cells, _, _ = workload_name(n)
+    prob = make_problem(n)
+    fe = prob.fes[0]
+    dev = torch.device("cuda")
+    t0 = time.perf_counter()
+    H, Hs = M.compute_filter_kd_tree(fe)
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    g = torch.Generator().manual_seed(1)
+    rho = (0.5 + 0.1 * (torch.rand(cells, 1, generator=g, dtype=torch.float64) - 0.5)).to(dev)
+    dJ = (-torch.rand(cells, 1, generator=g, dtype=torch.float64)).to(dev)
+    dvc = torch.full((1, cells, 1), 1.0 / (cells * 0.5), dtype=torch.float64, device=dev)
+    vc = np.array([rho.mean().item() / 0.5 - 1.0])
+    ft = {"H": H, "Hs": Hs}
+    mm = M.MMA()
+    mm.setNumConstraints(1)
+    mm.setNumDesignVariables(cells)
+    mm.setMinandMaxBoundsForDesignVariables(torch.zeros(cells, 1, dtype=torch.float64, device=dev),
+                                            torch.ones(cells, 1, dtype=torch.float64, device=dev))
+    mm.setScalingParams(1.0, np.zeros(1), 1e4 * np.ones(1), np.zeros(1))
+    mm.setMoveLimit(0.1)
+
+    def one():
+        dJf, dvcf = M.applySensitivityFilter(ft, rho, dJ, dvc)
+        mm.epoch = 1
+        mm.xold1, mm.xold2 = rho, rho
+        mm.setLowerAndUpperAsymptotes(torch.ones_like(rho), torch.ones_like(rho))
+        mm.setObjectiveWithGradient(0.0, dJf.reshape(-1, 1))
+        mm.setConstraintWithGradient(vc, dvcf.reshape(1, -1))
+        mm.mmasub(rho)
+    for _ in range(max(args.warmup, 1)):
+        one()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    launches0 = jf._lib.load().fem_kernel_launches()
+    ev[0].record()
+    for _ in range(args.steps):
+        one()
+    ev[1].record()
+    torch.cuda.synchronize()
+    t_gpu = ev[0].elapsed_time(ev[1]) / 1e3 / args.steps
+    launches = (jf._lib.load().fem_kernel_launches() - launches0) // max(args.steps, 1)
+    xg = mm.xmma.cpu().numpy().reshape(-1)
+    cpu = None
+    if not args.no_cpu:
+        from oracle import mma as omma
+        cent = np.mean(fe.points[fe.cells], axis=1)
+        t0 = time.perf_counter()
+        Ho, Hso, _ = omma.filter_kd_tree(cent, M._cell_volume(fe))
+        t_cpu_build = time.perf_counter() - t0
+        r, d0, dv = rho.cpu().numpy().reshape(-1), dJ.cpu().numpy().reshape(-1), dvc.cpu().numpy().reshape(1, -1)
+        t0 = time.perf_counter()
+        dJf, dvcf = omma.sensitivity_filter(Ho, Hso, r, d0, dv)
+        xr, _, _ = omma.mmasub(1, r, r, r, np.ones(cells), np.ones(cells), np.zeros(cells), np.ones(cells), 0.1,
+                               0.0, dJf, vc, dvcf, 1.0, np.zeros(1), 1e4 * np.ones(1), np.zeros(1))
+        t_cpu = time.perf_counter() - t0
+        cpu = {"value": t_cpu, "unit": "s/update", "cores": 1, "kind": "port",
+               "sample": f"oracle numpy/scipy filter product + mmasub on the same {cells} variables (full size); "
+                         f"k-d tree filter build {t_cpu_build:.1f} s (GPU build {t_build:.2f} s)",
+               "max_abs_diff_vs_gpu": float(np.abs(xr - xg).max())}
+    line = {"metric": "TO update (sensitivity filter + MMA) s/update", "value": t_gpu, "unit": "s/update",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{cells} design cells of {name}, m=1 volume constraint, move 0.1"},
+            "newton_steps": mm.newton_steps, "gpu_launches_per_update": int(launches), "cpu_baseline": cpu}
+    print(json.dumps(line))
+
+
 def _default_iters(n):
     # Jacobi-PCG iterations grow ~linearly with the longest mesh dimension for this cantilever
     return (int(12 * max(n)), int(12 * max(n)))
@@ -349,11 +426,16 @@ def main():
     ap.add_argument("--size", type=int, nargs=3, default=list(DEFAULT_SIZE))
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--mma-update", action="store_true",
+                    help="time the TO update (filter + MMA) beside the step and print its own JSON line")
     ap.add_argument("--kernel-shares", action="store_true",
                     help="print per-kernel device time of one step per precision (CUPTI trace) and exit")
     args = ap.parse_args()
     if args.kernel_shares:
         kernel_shares(args)
+        return
+    if args.mma_update:
+        mma_update_bench(args)
         return
 
     rank = int(os.environ.get("RANK", "0"))

@@ -159,6 +159,16 @@ int fem_body_load(const fem_mesh_t* mesh, const double* f_qp, double* out, void*
 /* out[dof] += sum_q t_qp[f,q,:] N_a(q) nanson  (surface_map at face quad points) */
 int fem_surface_load(const fem_mesh_t* mesh, const int32_t* face_cells, const int32_t* face_ids,
                      int64_t n_faces, const double* t_qp, double* out, void* stream);
+/* u-dependent surface maps (problem.py:238-259 with a u-dependent surface_map; Robin,
+ * applications/robin_bc/example.py:64-80): t_v(u, x) = h_v(x) + sum_{k=1..degree} c[v][k] u_v^k,
+ * coeffs (host) = c as vec x (degree+1) (column 0 unused: h goes through fem_surface_load).
+ * outputs: FEM_OUT_RESIDUAL adds sum_q t N_a nanson to residual; FEM_OUT_MATRIX adds
+ * dt/du N_a N_b nanson to vals (FEM_F32 / FEM_F64, BC rows / columns as fem_assemble's bc_mode);
+ * FEM_OUT_APPLY adds the tangent action on w to apply_out.  1 <= degree <= 4. */
+int fem_surface_robin(const fem_mesh_t* mesh, const fem_pattern_t* pat, const int32_t* face_cells,
+                      const int32_t* face_ids, int64_t n_faces, int32_t degree, const double* coeffs,
+                      int32_t outputs, int32_t precision, const double* u, const double* w, const uint8_t* bc_mask,
+                      int32_t bc_mode, double* residual, void* vals, double* apply_out, void* stream);
 
 /* ---- per-cell weak form and assembly --------------------------------------
  * Replaces the cell kernels and their jacfwd tangents jax_fem/problem.py:189-303,

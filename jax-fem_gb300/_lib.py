@@ -72,6 +72,7 @@ SIGNATURES = {
     "fem_face_quad_points": ([PMESH, P, P, I64, P, P, P], C.c_int),
     "fem_body_load": ([PMESH, P, P, P], C.c_int),
     "fem_surface_load": ([PMESH, P, P, I64, P, P, P], C.c_int),
+    "fem_surface_robin": ([PMESH, PPAT, P, P, I64, I32, PF64, I32, I32, P, P, P, I32, P, P, P, P], C.c_int),
     "fem_assemble": ([PMESH, PMAT, PPAT, I32, I32, P, P, P, I32, P, P, P, P], C.c_int),
     "fem_param_vjp": ([PMESH, PMAT, P, P, P, P, P], C.c_int),
     "fem_j2_update": ([PMESH, PMAT, P, P, P], C.c_int),

@@ -382,3 +382,119 @@ extern "C" int fem_j2_history_vjp(const fem_mesh_t* mesh, const fem_material_t* 
   P.res = u_grad;
   return run_cell_kernel(mesh, P, mat->kind, FEM_F64, KMODE_HVJP, as_stream(stream));
 }
+
+// ---- u-dependent (Robin) surface maps -------------------------------------------------
+// Surface map t_v(u, x) = h_v(x) + sum_{k=1..deg} c[v][k] u_v^k on the selected faces
+// (problem.py:238-259 with a u-dependent surface_map; applications/robin_bc/example.py:64-80).
+// The x-only part h goes into the load vector (fem_surface_load); this kernel adds the
+// u-dependent part to the residual, its tangent dt/du N_a N_b nanson to the CSR values (same
+// slots as the cell kernel) and/or its action on w.  Thread per (face, node, component).
+namespace fem {
+
+struct RobinCoef {
+  double c[3][5];
+  int deg;
+};
+
+template <typename T>
+__global__ void robin_kernel(FaceTables ft, int vec, const double* coords, const int32_t* conn,
+                             const int32_t* face_cells, const int32_t* face_ids, int64_t n_faces, RobinCoef rc,
+                             const double* u, const double* w, const uint8_t* bc, int bc_mode, int outputs,
+                             double* res, T* vals, double* apply_out, const int64_t* indptr, const uint8_t* slots) {
+  const int NN = ft.nn, NFQ = ft.nfq;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_faces * NN * vec;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int v = (int)(k % vec);
+    const int a = (int)((k / vec) % NN);
+    const int64_t f = k / ((int64_t)vec * NN);
+    const int64_t e = face_cells[f];
+    const int fid = face_ids[f];
+    const int na = conn[e * NN + a];
+    const int64_t row = (int64_t)na * vec + v;
+    const bool row_bc = bc && bc[row];
+    double r = 0.0, ap = 0.0, kb[MAX_NN];
+    for (int b = 0; b < NN; ++b) kb[b] = 0.0;
+    bool on_face = false;
+    for (int q = 0; q < NFQ; ++q) {
+      const double Na = ft.N[fid][q][a];
+      if (Na == 0.0) continue;
+      on_face = true;
+      double J[3][3] = {}, uq = 0.0, wq = 0.0;
+      for (int n = 0; n < NN; ++n) {
+        const int node = conn[e * NN + n];
+        for (int d = 0; d < 3; ++d) {
+          const double X = coords[(int64_t)node * 3 + d];
+          for (int s = 0; s < 3; ++s) J[d][s] += X * ft.dN[fid][q][n][s];
+        }
+        const double Nn = ft.N[fid][q][n];
+        const int64_t dof = (int64_t)node * vec + v;
+        uq += Nn * u[dof];
+        if (w) wq += Nn * ((bc && bc[dof] && bc_mode == FEM_BC_SYMMETRIC) ? 0.0 : w[dof]);
+      }
+      const double det = det3<double>(J);
+      double Ji[3][3];
+      inv3<double>(J, det, Ji);
+      double v3[3];
+      for (int d = 0; d < 3; ++d)
+        v3[d] = ft.normal[fid][0] * Ji[0][d] + ft.normal[fid][1] * Ji[1][d] + ft.normal[fid][2] * Ji[2][d];
+      const double nanson = sqrt(v3[0] * v3[0] + v3[1] * v3[1] + v3[2] * v3[2]) * det * ft.w[fid][q];
+      double t = 0.0, dt = 0.0, pk = 1.0;   // pk = u^(k-1)
+      for (int p = 1; p <= rc.deg; ++p) {
+        dt += p * rc.c[v][p] * pk;
+        pk *= uq;
+        t += rc.c[v][p] * pk;
+      }
+      r += t * Na * nanson;
+      ap += dt * wq * Na * nanson;
+      for (int b = 0; b < NN; ++b) kb[b] += dt * Na * ft.N[fid][q][b] * nanson;
+    }
+    if (!on_face) continue;
+    if ((outputs & FEM_OUT_RESIDUAL) && res) atomicAdd(res + row, r);
+    if ((outputs & FEM_OUT_APPLY) && apply_out && !row_bc) atomicAdd(apply_out + row, ap);
+    if ((outputs & FEM_OUT_MATRIX) && vals && !(row_bc && bc_mode != FEM_BC_NONE)) {
+      const int64_t rs = indptr[row];
+      const uint8_t* sl = slots + (e * NN + a) * NN;
+      for (int b = 0; b < NN; ++b) {
+        if (kb[b] == 0.0) continue;
+        const int nb = conn[e * NN + b];
+        if (bc_mode == FEM_BC_SYMMETRIC && bc && bc[(int64_t)nb * vec + v]) continue;
+        atomicAdd(vals + rs + (int64_t)vec * sl[b] + v, T(kb[b]));
+      }
+    }
+  }
+}
+
+}  // namespace fem
+
+extern "C" int fem_surface_robin(const fem_mesh_t* mesh, const fem_pattern_t* pat, const int32_t* face_cells,
+                                 const int32_t* face_ids, int64_t n_faces, int32_t degree, const double* coeffs,
+                                 int32_t outputs, int32_t precision, const double* u, const double* w,
+                                 const uint8_t* bc_mask, int32_t bc_mode, double* residual, void* vals,
+                                 double* apply_out, void* stream) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  FEM_REQUIRE(n_faces >= 0 && degree >= 1 && degree <= 4, "need n_faces >= 0 and 1 <= degree <= 4");
+  FEM_REQUIRE(coeffs && u, "NULL argument");
+  FEM_REQUIRE(!(outputs & FEM_OUT_MATRIX) || (pat && vals && pat->indptr && pat->slots), "matrix output needs a pattern");
+  FEM_REQUIRE(!(outputs & FEM_OUT_APPLY) || (w && apply_out), "APPLY needs w and apply_out");
+  FEM_REQUIRE(precision == FEM_F32 || precision == FEM_F64, "values must be FEM_F32 or FEM_F64");
+  if (n_faces == 0) return FEM_OK;
+  FEM_REQUIRE(face_cells && face_ids, "face arrays NULL");
+  RobinCoef co{};
+  co.deg = degree;
+  for (int v = 0; v < mesh->vec; ++v)
+    for (int p = 0; p <= degree; ++p) co.c[v][p] = coeffs[v * (degree + 1) + p];
+  FaceTables ft = make_face_tables(mesh->elem_type);
+  const int64_t work = n_faces * ft.nn * mesh->vec;
+  cudaStream_t s = as_stream(stream);
+  if (precision == FEM_F32)
+    robin_kernel<float><<<grid_for(work, 128), 128, 0, s>>>(
+        ft, mesh->vec, mesh->coords, mesh->conn, face_cells, face_ids, n_faces, co, u, w, bc_mask, bc_mode, outputs,
+        residual, static_cast<float*>(vals), apply_out, pat ? pat->indptr : nullptr, pat ? pat->slots : nullptr);
+  else
+    robin_kernel<double><<<grid_for(work, 128), 128, 0, s>>>(
+        ft, mesh->vec, mesh->coords, mesh->conn, face_cells, face_ids, n_faces, co, u, w, bc_mask, bc_mode, outputs,
+        residual, static_cast<double*>(vals), apply_out, pat ? pat->indptr : nullptr, pat ? pat->slots : nullptr);
+  note_launches(1);
+  return check_launch("robin_kernel");
+}

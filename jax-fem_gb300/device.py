@@ -142,6 +142,27 @@ class Engine:
         self._ws = {}
         self.f_ext = torch.zeros(self.num_dofs, dtype=torch.float64, device=dev)
         self._loads_done = False
+        self._robin = []            # (face_cells, face_ids, degree, coeffs) of u-dependent surface maps
+
+    def add_robin(self, boundary_inds, coeffs):
+        """Register the u-dependent polynomial part of a surface map on the faces boundary_inds."""
+        bi = np.asarray(boundary_inds)
+        fc = torch.as_tensor(bi[:, 0].astype(np.int32), device=self.device)
+        fi = torch.as_tensor(bi[:, 1].astype(np.int32), device=self.device)
+        co = np.ascontiguousarray(np.asarray(coeffs, dtype=np.float64))
+        self._robin.append((fc, fi, co.shape[1] - 1, co))
+        self._tangent_cache.clear()
+
+    @property
+    def robin_linear(self):
+        return all(deg <= 1 for _, _, deg, _ in self._robin)
+
+    def _robin_call(self, outputs, precision, dofs, w=None, bc_mode=_lib.FEM_BC_NONE, bc=None, res=None, vals=None,
+                    apply_out=None):
+        for fc, fi, deg, co in self._robin:
+            call("fem_surface_robin", C.byref(self.mesh), C.byref(self.pattern), ptr(fc), ptr(fi), fc.numel(), deg,
+                 co.ctypes.data_as(C.POINTER(C.c_double)), outputs, precision, ptr(dofs), ptr(w), ptr(bc), bc_mode,
+                 ptr(res), ptr(vals), ptr(apply_out), _stream())
 
     # ---- pattern -------------------------------------------------------------------
     def _build_pattern(self):
@@ -291,6 +312,8 @@ class Engine:
         dofs = dofs.contiguous()
         call("fem_assemble", C.byref(self.mesh), C.byref(ms), C.byref(self.pattern), _lib.FEM_OUT_RESIDUAL,
              _lib.FEM_F64, ptr(dofs), None, None, _lib.FEM_BC_NONE, ptr(res), None, None, _stream())
+        if self._robin:
+            self._robin_call(_lib.FEM_OUT_RESIDUAL, _lib.FEM_F64, dofs, res=res)
         if apply_bc:
             self.refresh_bc()
             if self.n_bc:
@@ -304,7 +327,7 @@ class Engine:
         self.refresh_bc()
         m, ms = self.material()
         key = (precision, bc_mode)
-        if cache and m.linear and key in self._tangent_cache:
+        if cache and m.linear and self.robin_linear and key in self._tangent_cache:
             return self._tangent_cache[key]
         if precision not in (_lib.FEM_F32, _lib.FEM_F64):
             # solver copies (DF48, sliced FP32 / FP64 / DF48) are converted from the FP64 CSR tangent
@@ -333,6 +356,8 @@ class Engine:
         dofs = dofs.contiguous()
         call("fem_assemble", C.byref(self.mesh), C.byref(ms), C.byref(self.pattern), _lib.FEM_OUT_MATRIX,
              precision, ptr(dofs), None, ptr(self.bc_mask), bc_mode, None, ptr(vals), None, _stream())
+        if self._robin:
+            self._robin_call(_lib.FEM_OUT_MATRIX, precision, dofs, bc_mode=bc_mode, bc=self.bc_mask, vals=vals)
         if bc_mode != _lib.FEM_BC_NONE and self.n_bc:
             call("fem_zero_rows", C.byref(self.pattern), self.vec, precision, ptr(vals), ptr(self.bc_rows), self.n_bc,
                  1.0, _stream())
@@ -348,6 +373,9 @@ class Engine:
         call("fem_assemble", C.byref(self.mesh), C.byref(ms), C.byref(self.pattern), _lib.FEM_OUT_APPLY,
              _lib.FEM_F64, ptr(dofs.contiguous()), ptr(w.contiguous()), ptr(self.bc_mask) if skip_bc_rows else None,
              _lib.FEM_BC_NONE, None, None, ptr(out), _stream())
+        if self._robin:
+            self._robin_call(_lib.FEM_OUT_APPLY, _lib.FEM_F64, dofs.contiguous(), w=w.contiguous(),
+                             bc=self.bc_mask if skip_bc_rows else None, apply_out=out)
         return out
 
     def param_vjp(self, dofs, lam):

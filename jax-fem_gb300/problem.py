@@ -103,7 +103,10 @@ class Problem:
                 continue
             xf, _ = eng.face_quad_points(bi)
             x = xf.reshape(-1, 3).cpu().numpy()
-            self._surface_tractions.append(_u_independent(fn, x, fe.vec, "surface map"))
+            h, coeffs = _surface_map_split(fn, x, fe.vec)
+            self._surface_tractions.append(h)
+            if coeffs is not None:
+                eng.add_robin(bi, coeffs)
         eng.refresh_loads()
 
     def _resolve_material(self):
@@ -140,6 +143,56 @@ def _flat(sol_list, device):
             raise NotImplementedError("single-variable problems only")
         sol_list = sol_list[0]
     return torch.as_tensor(sol_list, dtype=torch.float64, device=device).reshape(-1).contiguous()
+
+
+def _surface_map_split(fn, x, vec, max_degree=4):
+    """Split a surface map t(u, x) into h(x) = t(0, x) at the face quadrature points and, when t
+    depends on u, component-wise polynomial coefficients c[v][k] (k = 0..deg, c[v][0] = 0) with
+    t_v(u, x) = h_v(x) + sum_k c[v][k] u_v^k, found by probing and verified on random u.  Other
+    u-dependence raises NotImplementedError.  Returns (h flat, coeffs (vec, deg+1) or None)."""
+    P = len(x)
+    h = eval_pointwise(lambda u, xx: fn(u, xx), [np.zeros((P, vec)), x], (vec,)).reshape(P, vec)
+    rng = np.random.default_rng(7)
+    probe = rng.integers(0, P, size=min(P, 3))
+    t = lambda u, p: np.asarray(fn(np.asarray(u, dtype=np.float64), x[p]), dtype=np.float64).reshape(vec)
+    if all(np.allclose(t(rng.standard_normal(vec), p), h[p], rtol=1e-12, atol=1e-12 * (np.abs(h[p]).max() + 1.0))
+           for p in probe):
+        return h.reshape(-1), None
+    samples = np.array([-1.0, -0.5, 0.5, 1.0, 1.5, 2.0])
+    V = samples[:, None] ** np.arange(1, max_degree + 1)[None, :]
+    coeffs = np.zeros((vec, max_degree + 1))
+    for v in range(vec):
+        fits = []
+        for p in probe:
+            rows = []
+            for sv in samples:
+                u = np.zeros(vec)
+                u[v] = sv
+                tv = t(u, p) - h[p]
+                others = np.delete(tv, v)
+                if not np.allclose(others, 0.0, atol=1e-12 * (np.abs(tv).max() + 1.0)):
+                    raise NotImplementedError("u-dependent surface maps must act component-wise")
+                rows.append(tv[v])
+            c, *_ = np.linalg.lstsq(V, np.array(rows), rcond=None)
+            fits.append(c)
+        fits = np.array(fits)
+        if not np.allclose(fits, fits[0], rtol=1e-9, atol=1e-12 * (np.abs(fits).max() + 1.0)):
+            raise NotImplementedError("the u-dependent part of a surface map must not depend on x")
+        coeffs[v, 1:] = fits[0]
+    scale = np.abs(coeffs).max()
+    if scale == 0.0:
+        raise NotImplementedError("u-dependent surface maps must act component-wise")
+    coeffs[np.abs(coeffs) <= 1e-13 * scale] = 0.0
+    deg = max(int(np.nonzero(np.abs(coeffs).max(0))[0].max()), 1)
+    coeffs = coeffs[:, :deg + 1]
+    for p in probe:
+        u = rng.uniform(-1.5, 1.5, vec)
+        pred = h[p] + np.array([np.polyval(coeffs[v][::-1], u[v]) for v in range(vec)])
+        if not np.allclose(t(u, p), pred, rtol=1e-9, atol=1e-11 * (np.abs(pred).max() + 1.0)):
+            raise NotImplementedError("only component-wise polynomial u-dependence (degree <= 4) is built for "
+                                      "surface maps")
+    logger.debug("surface map: u-dependent part of degree %d", deg)
+    return h.reshape(-1), coeffs
 
 
 def _u_independent(fn, x, vec, what):

@@ -148,3 +148,24 @@ def test_pointwise_eval_falls_back(lib):
     np.testing.assert_allclose(eval_pointwise(f2, [x], (3,)), -x * np.array([1e3, 2e3, 3e3]))
     f3 = lambda p: np.array([0.0, 10.0, 10.0])
     assert eval_pointwise(f3, [x], (3,)).shape == (20, 3)
+
+
+def test_surface_map_split_probe():
+    """u-dependent surface maps: component-wise polynomials (here the Robin example's 5 u^2 and a
+    linear spring with an x-dependent load) are split into h(x) + sum_k c_k u^k; non-polynomial
+    or coupled u-dependence is refused loudly."""
+    import importlib
+    import numpy as np
+    import pytest
+    P = importlib.import_module("jax_fem_gb300.problem")
+    x = np.random.default_rng(0).uniform(0, 1, (12, 3))
+    h, c = P._surface_map_split(lambda u, xx: 5.0 * u ** 2, x, 1)
+    assert np.allclose(h, 0.0) and c.shape == (1, 3) and np.allclose(c, [[0, 0, 5.0]])
+    h, c = P._surface_map_split(lambda u, xx: 100.0 * u + np.array([0.0, 0.0, -xx[0]]), x, 3)
+    assert np.allclose(h.reshape(-1, 3)[:, 2], -x[:, 0]) and c.shape == (3, 2) and np.allclose(c[:, 1], 100.0)
+    h, c = P._surface_map_split(lambda u, xx: np.array([0.0, 1.0, 2.0]), x, 3)
+    assert c is None and np.allclose(h.reshape(-1, 3), [0.0, 1.0, 2.0])
+    with pytest.raises(NotImplementedError):
+        P._surface_map_split(lambda u, xx: np.sin(u), x, 1)
+    with pytest.raises(NotImplementedError):
+        P._surface_map_split(lambda u, xx: np.array([u[0] * u[1], 0.0, 0.0]), x, 3)
