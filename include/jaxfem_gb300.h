@@ -331,6 +331,25 @@ int fem_filter_build(int64_t n, const double* centroids, double rmin, int32_t nn
 int fem_filter_apply(int64_t n, int32_t nnb, const int32_t* cols, const double* vals, const double* hs,
                      const double* rho, const double* g, int32_t nr, int32_t mode, double* out, void* stream);
 
+/* ---- dynamic relaxation (jax_fem/solver.py:918-1049) --------------------------------- */
+/* out[r] = scale * sum_k |vals[k]| over scalar CSR row r (lumped mass of assembleCSR's matrix,
+ * solver.py:959-961, with scale = h~^2/4). */
+int fem_row_abs_sum(int64_t n_rows, const int64_t* indptr, const double* vals, double scale, double* out,
+                    void* stream);
+/* q_old = q; R_old = R; q += h qdot (solver.py:983-985). */
+int fem_dr_march(int64_t n, double h, double* q, double* q_old, const double* qdot, const double* R, double* R_old,
+                 void* stream);
+/* out4 (host) = [max|R|, sum (R - R_old)/h qdot, sum qdot M qdot,
+ *                max h~^2/4 |(qdd - qdd_old)/(q - q_old)| over q != q_old] (solver.py:991-1002);
+ * ws: device scratch of at least 8*(4*2048+4) bytes.  Synchronises the stream. */
+int fem_dr_measure(int64_t n, double h, double h_tilde, const double* R, const double* R_old, const double* qdot,
+                   const double* M, const double* q, const double* q_old, const double* qdd, const double* qdd_old,
+                   double* out4, double* ws, size_t ws_bytes, void* stream);
+/* qdot_old = qdot; qdd_old = qdd; qdot = (2 - c h)/(2 + c h) qdot_old - 2h/(2 + c h) R/M;
+ * qdd = (qdot - qdot_old)/h (solver.py:1020-1022). */
+int fem_dr_velocity(int64_t n, double h, double c, const double* R, const double* M, double* qdot, double* qdot_old,
+                    double* qdd, double* qdd_old, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

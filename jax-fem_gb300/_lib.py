@@ -95,6 +95,10 @@ SIGNATURES = {
     "fem_cast_f64_f32": ([P, P, I64, P, P], C.c_int),
     "fem_axpy_f32_f64": ([F64, P, P, I64, P], C.c_int),
     "fem_dot": ([I32, P, P, I64, P, P, SZ, P], C.c_int),
+    "fem_row_abs_sum": ([I64, P, P, F64, P, P], C.c_int),
+    "fem_dr_march": ([I64, F64, P, P, P, P, P, P], C.c_int),
+    "fem_dr_measure": ([I64, F64, F64, P, P, P, P, P, P, P, P, PF64, P, SZ, P], C.c_int),
+    "fem_dr_velocity": ([I64, F64, F64, P, P, P, P, P, P, P], C.c_int),
     "fem_mma_workspace": ([I64, I32, PSZ], C.c_int),
     "fem_mma_update": ([I64, I32, I32, P, P, P, P, P, P, P, F64, P, PF64, P, F64, PF64, PF64, PF64, P, P, SZ, PI32, P],
                        C.c_int),

@@ -205,6 +205,6 @@ def _u_independent(fn, x, vec, what):
     for p in probe:
         alt = np.asarray(fn(rng.standard_normal(vec), x[p]), dtype=np.float64).reshape(vec)
         if not np.allclose(alt, val[p], rtol=1e-12, atol=1e-12 * (np.abs(val[p]).max() + 1.0)):
-            raise NotImplementedError(f"{what} depends on u; u-dependent (Robin) maps are not part of this build")
+            raise NotImplementedError(f"{what} depends on u; only u-independent {what}s are built")
     logger.debug("%s evaluated at %d points", what, P)
     return val.reshape(-1)

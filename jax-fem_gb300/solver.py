@@ -239,8 +239,19 @@ def _line_search(problem, eng, dofs, inc):
 def solver(problem, solver_options={}):
     """Newton solve (solver.py:1112-1356).  Returns sol_list = [tensor (num_nodes, vec)] (FP64, device)."""
     method, cfg = _resolve_solver_options(solver_options)
-    if method != "newton":
-        raise NotImplementedError(f"'{method}' is not part of this build (Newton only)")
+    if method == "arc_length":
+        from .drivers import solve_arc_length
+        sol_list, info = solve_arc_length(problem, cfg)
+        return (sol_list, info) if cfg.get("return_info", False) else sol_list
+    if method == "dynamic_relax":
+        from .drivers import dynamic_relax_solve
+        ig = cfg.get("initial_guess")
+        if ig is not None:
+            ig = _flat_v(ig, problem._engine.device)
+        return dynamic_relax_solve(problem, tol=cfg.get("tol", 1e-6), nKMat=cfg.get("nKMat", 1000),
+                                   nPrint=cfg.get("nPrint", 500), info=cfg.get("info", True),
+                                   info_force=cfg.get("info_force", True), initial_guess=ig,
+                                   linear_options=cfg.get("linear", {}), max_iters=cfg.get("max_iters"))
     eng = problem._engine
     spec = resolve_linear(cfg.get("linear", {}))
     precision = _precision(cfg)
@@ -497,6 +508,13 @@ def update_j2_history(problem, sol, sigmas_old, epsilons_old, scale=None):
 
 
 # ---- BC helpers of the reference, device versions (solver.py:290-363) ----------------
+def get_q_vec(problem):
+    """solver.py:637-642: the residual at u = 0 without Dirichlet rows (force-controlled
+    arc-length's reference load)."""
+    eng = problem._engine
+    return eng.residual(torch.zeros(eng.num_dofs, dtype=torch.float64, device=eng.device), apply_bc=False)
+
+
 def apply_bc_vec(res_vec, dofs, problem, scale=1.0):
     eng = problem._engine
     eng.refresh_bc()
