@@ -13,10 +13,11 @@ from .materials import (GeneralLinear, J2Plasticity, Laplace, LinearElastic, Mat
                         SIMPElastic)
 from .logger import logger
 from .problem import Problem
+from .utils import read_vtu, save_sol
 from .solver import (ad_wrapper, adjoint_solve, apply_bc_vec, assign_bc, copy_bc, get_A, implicit_vjp,
                      linear_solver, solver, update_j2_history, get_q_vec)
 
-__all__ = ["Problem", "solver", "ad_wrapper", "implicit_vjp", "update_j2_history", "get_q_vec", "linear_solver", "get_A", "apply_bc_vec",
+__all__ = ["save_sol", "read_vtu", "Problem", "solver", "ad_wrapper", "implicit_vjp", "update_j2_history", "get_q_vec", "linear_solver", "get_A", "apply_bc_vec",
            "assign_bc", "copy_bc", "adjoint_solve", "Mesh", "box_mesh", "box_mesh_tet10", "get_meshio_cell_type",
            "Laplace", "LinearElastic", "SIMPElastic", "GeneralLinear", "NeoHookean", "J2Plasticity", "Material",
            "logger", "build"]

@@ -102,6 +102,17 @@ class DeviceCSR:
         """torch sparse CSR view (debugging / custom solvers)."""
         return torch.sparse_csr_tensor(self.indptr, self.indices.to(torch.int64), self.data, size=self.shape)
 
+    # PETSc Mat methods used by the reference's custom_solver plug-ins (solver.py:278-280; the
+    # documented example converts with A.getValuesCSR() / A.getSize())
+    def getValuesCSR(self):
+        """(indptr, indices, data) host arrays of the FP64 values (int32 indices as PETSc)."""
+        src = self if self.source is None else self.source
+        return (src.indptr.cpu().numpy().astype(np.int32), src.indices.cpu().numpy().astype(np.int32),
+                src.data.double().cpu().numpy())
+
+    def getSize(self):
+        return self.shape
+
     def to_scipy(self):
         """Host copy as scipy CSR (for user code and tests only)."""
         import scipy.sparse as sp

@@ -169,3 +169,29 @@ def test_surface_map_split_probe():
         P._surface_map_split(lambda u, xx: np.sin(u), x, 1)
     with pytest.raises(NotImplementedError):
         P._surface_map_split(lambda u, xx: np.array([u[0] * u[1], 0.0, 0.0]), x, 3)
+
+
+@pytest.mark.parametrize("binary", [True, False])
+def test_save_sol_vtu_round_trip(tmp_path, binary):
+    """save_sol (utils.py:13-57) writes a VTU whose points, cells, 'sol' (float32) and cell /
+    point data read back unchanged, for HEX8 and TET10 meshes."""
+    import importlib
+    import numpy as np
+    jf = importlib.import_module("jax_fem_gb300")
+    U = importlib.import_module("jax_fem_gb300.utils")
+    FE = importlib.import_module("jax_fem_gb300.fe")
+    for m, et, key in ((jf.box_mesh(3, 2, 2, 1.0, 1.0, 1.0), "HEX8", "hexahedron"),
+                       (jf.box_mesh_tet10(2, 2, 1, 1.0, 1.0, 1.0), "TET10", "tetra10")):
+        fe = FE.FiniteElement(jf.Mesh(m.points, m.cells_dict[key]), vec=3, dim=3, ele_type=et)
+        rng = np.random.default_rng(0)
+        sol = rng.standard_normal((fe.num_total_nodes, 3))
+        theta = rng.uniform(size=fe.num_cells)
+        T = rng.uniform(size=fe.num_total_nodes)
+        path = tmp_path / f"{et}_{binary}.vtu"
+        U.save_sol(fe, sol, str(path), cell_infos=[("theta", theta)], point_infos=[("T", T)], binary=binary)
+        pts, cells, pd, cd = U.read_vtu(str(path))
+        np.testing.assert_array_equal(pts, fe.points)
+        np.testing.assert_array_equal(cells[key], fe.cells)
+        np.testing.assert_array_equal(pd["sol"], sol.astype(np.float32))
+        np.testing.assert_array_equal(pd["T"], T.astype(np.float32))
+        np.testing.assert_array_equal(cd["theta"], theta.astype(np.float32))

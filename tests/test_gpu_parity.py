@@ -417,3 +417,24 @@ def test_spmv_dfx_matches_fp64(cuda, n):
         assert (y - y64).abs().max().item() <= 1e-11 * y64.abs().max().item()
         ref = torch.dot(x, y64).item()
         assert abs(dot.item() - ref) <= 1e-11 * abs(ref)
+
+
+def test_custom_solver_hook_petsc_style(cuda):
+    """custom_solver plug-in (solver.py:278-280) written against the PETSc Mat interface of the
+    documented example (A.getValuesCSR(), A.getSize(); scipy direct solve on the host) gives the
+    built-in solve's solution on the cube case (1e-10)."""
+    import scipy.sparse
+    import scipy.sparse.linalg
+    import jax_fem_gb300 as jf
+    import cases
+
+    def host_direct(A, b, x0, opts):
+        indptr, indices, data = A.getValuesCSR()
+        As = scipy.sparse.csr_array((data, indices, indptr), shape=A.getSize())
+        return scipy.sparse.linalg.spsolve(As.tocsc(), b.cpu().numpy())
+
+    prob, _ = cases.cube_elasticity(golden("linear_elasticity_cube"))[:2]
+    ref = jf.solver(prob, {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-13},
+                           "rel_tol": 1e-12, "tol": 0.0})[0]
+    got = jf.solver(prob, {"custom_solver": host_direct, "rel_tol": 1e-12, "tol": 0.0})[0]
+    assert (got - ref).abs().max().item() <= 1e-10 * ref.abs().max().item()
