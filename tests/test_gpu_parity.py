@@ -435,6 +435,6 @@ def test_custom_solver_hook_petsc_style(cuda):
 
     prob, _ = cases.cube_elasticity(golden("linear_elasticity_cube"))[:2]
     ref = jf.solver(prob, {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-13},
-                           "rel_tol": 1e-12, "tol": 0.0})[0]
-    got = jf.solver(prob, {"custom_solver": host_direct, "rel_tol": 1e-12, "tol": 0.0})[0]
+                           "rel_tol": 1e-10, "tol": 0.0})[0]
+    got = jf.solver(prob, {"custom_solver": host_direct, "rel_tol": 1e-10, "tol": 0.0})[0]
     assert (got - ref).abs().max().item() <= 1e-10 * ref.abs().max().item()
