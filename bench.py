@@ -302,6 +302,21 @@ def bench_reference(args):
     print(json.dumps(line))
 
 
+def max_over_ranks(t, dist=None, device="cuda"):
+    """The slowest rank's time (replicas: every rank runs its own copy of the workload)."""
+    if dist is None:
+        return t
+    import torch
+    tt = torch.tensor([t], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_seconds_per_iter(t_max, steps, world):
+    """Whole-job s/iter with `world` replicas each running `steps` iterations in t_max seconds."""
+    return t_max / (steps * world)
+
+
 def kernel_shares(args):
     """Per-kernel device time of one warm TO step in each precision, from a CUPTI activity trace
     (torch.profiler): launches, total, share and time per launch.  A profile, not a bench line."""
@@ -487,11 +502,7 @@ def main():
         e1.record(s)
         barrier()
         launches = lib.fem_kernel_launches() - l0
-        t = e0.elapsed_time(e1) / 1e3
-        if dist is not None:
-            tt = torch.tensor([t], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            t = tt.item()
+        t = max_over_ranks(e0.elapsed_time(e1) / 1e3, dist, "cuda")
         its = [r["iterations"] for r in eng.solve_log]
         return t, out, launches, its, dict(eng.timing)
 
@@ -542,7 +553,7 @@ def main():
 
     f32 = roof.get("df48", roof.get("fp32", {}))
     traffic = traffic_from_profile(nnz)
-    value = t_mx / args.steps / world
+    value = job_seconds_per_iter(t_mx, args.steps, world)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_mx / args.steps * 1e3, "higher_is_better": False,
