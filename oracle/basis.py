@@ -113,6 +113,14 @@ def tet10_shape(xi):
     return vals, grads
 
 
+def tet4_shape(xi):
+    """Linear tetrahedron (basis.py:55-60, degree 1): barycentric shape functions."""
+    xi = np.atleast_2d(xi)
+    vals = np.stack([1 - xi.sum(1), xi[:, 0], xi[:, 1], xi[:, 2]], axis=1)
+    dL = np.array([[-1, -1, -1], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=np.float64)
+    return vals, np.broadcast_to(dL, (len(xi), 4, 3)).copy()
+
+
 def tet_quadrature(order=2):
     if order == 2:
         a, b = 0.5854101966249685, 0.1381966011250105
@@ -162,6 +170,14 @@ def element_tables(ele_type, quadrature_order=None):
         fpts, fw = tet_face_quadrature(order)
         nf, nfq, _ = fpts.shape
         fv, fg = tet10_shape(fpts.reshape(-1, 3))
+        face_inds, normals = TET_FACE_INDS, TET_FACE_NORMALS
+    elif ele_type == "TET4":
+        order = 0 if quadrature_order is None else quadrature_order   # basis.py:59, one point
+        pts, w = tet_quadrature(order)
+        vals, grads = tet4_shape(pts)
+        fpts, fw = tet_face_quadrature(order)
+        nf, nfq, _ = fpts.shape
+        fv, fg = tet4_shape(fpts.reshape(-1, 3))
         face_inds, normals = TET_FACE_INDS, TET_FACE_NORMALS
     else:
         raise NotImplementedError(ele_type)

@@ -50,7 +50,7 @@ def test_argument_errors_without_gpu(lib):
 def test_element_tables_match_oracle(lib):
     from jax_fem_gb300 import basis
     from oracle import basis as ob
-    for e in ("HEX8", "TET10"):
+    for e in ("HEX8", "TET10", "TET4"):
         t, o = basis.element_tables(e), ob.element_tables(e)
         for k in ("shape_vals", "shape_grads_ref", "quad_weights", "face_shape_vals", "face_shape_grads_ref",
                   "face_quad_weights", "face_normals", "face_inds"):

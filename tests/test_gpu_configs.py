@@ -200,3 +200,36 @@ def test_j2_modulus_field_five_steps_gradient(cuda, n):
     fd = (Jp - Jm) / (2 * h)
     an = torch.dot(grad, v).item()
     assert abs(fd - an) <= 1e-4 * max(abs(fd), abs(an)), (fd, an)
+
+
+def test_tet4_pattern_values_solution_vs_oracle(cuda):
+    """TET4 (one-point rule, basis.py:55-60) on the Kuhn split of 4^3 cubes: CSR pattern
+    bit-exact, FP64 tangent 1e-12 and the stretch solution 1e-9 against the oracle."""
+    import jax_fem_gb300 as jf
+    from oracle import fem as ofem, materials as omat, solve as osolve
+    m = jf.box_mesh_tet10(4, 4, 4, 1.0, 1.0, 1.0)
+    nv = 5 ** 3
+    pts, cells = np.asarray(m.points)[:nv], np.asarray(m.cells_dict["tetra10"])[:, :4]
+    bc = _stretch_bc(1.0)
+    bc[2][3] = (lambda p: 0.01)
+
+    class P(jf.Problem):
+        def get_tensor_map(self):
+            return jf.LinearElastic(1.0, 0.3)
+
+    prob = P(jf.Mesh(pts, cells), vec=3, dim=3, ele_type="TET4", dirichlet_bc_info=bc)
+    oprob = ofem.OracleProblem(pts, cells, 3, ele_type="TET4", dirichlet_bc_info=bc,
+                               tensor_map=omat.linear_elastic(1.0, 0.3))
+    eng = prob._engine
+    ip, ix = ofem.coo_pattern(oprob.I, oprob.J, oprob.num_total_dofs_all_vars)
+    np.testing.assert_array_equal(eng.indptr.cpu().numpy(), ip)
+    np.testing.assert_array_equal(eng.scalar_indices().cpu().numpy(), ix)
+    u = np.random.default_rng(4).standard_normal(oprob.num_total_dofs_all_vars) * 1e-2
+    prob.newton_update([torch.tensor(u, device=cuda).reshape(-1, 3)])
+    A = jf.get_A(prob)
+    oprob.newton_update(torch.tensor(u))
+    Ao = ofem.assemble_petsc(oprob)
+    assert np.abs(A.data.cpu().numpy() - Ao.data).max() <= 1e-12 * np.abs(Ao.data).max()
+    ref = np.asarray(osolve.newton_solve(oprob, {"spsolve_solver": {}, "rel_tol": 1e-12, "tol": 0.0})).reshape(-1)
+    sol = jf.solver(prob, _newton_opts("fp64", 1e-10))[0].reshape(-1).cpu().numpy()
+    assert np.abs(sol - ref).max() <= 1e-9 * np.abs(ref).max()

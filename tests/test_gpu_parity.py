@@ -438,3 +438,18 @@ def test_custom_solver_hook_petsc_style(cuda):
                            "rel_tol": 1e-10, "tol": 0.0})[0]
     got = jf.solver(prob, {"custom_solver": host_direct, "rel_tol": 1e-10, "tol": 0.0})[0]
     assert (got - ref).abs().max().item() <= 1e-10 * ref.abs().max().item()
+
+
+def test_cube_gold_through_vtu_round_trip(cuda, tmp_path):
+    """The reference's regression flow (test_linear_elasticity_cube.py:45-83): solve, write the
+    solution with save_sol (float32 point data), read the file back and compare with the
+    FEniCSx gold at decimal 5."""
+    import jax_fem_gb300 as jf
+    import cases
+    g = golden("linear_elasticity_cube")
+    prob, _ = cases.cube_elasticity(g)
+    sol = jf.solver(prob, {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}})[0]
+    path = tmp_path / "u.vtu"
+    jf.save_sol(prob.fes[0], sol, str(path))
+    _, _, pd, _ = jf.read_vtu(str(path))
+    np.testing.assert_array_almost_equal(g["sol"], pd["sol"], decimal=5)
