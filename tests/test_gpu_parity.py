@@ -422,7 +422,7 @@ def test_spmv_dfx_matches_fp64(cuda, n):
 def test_custom_solver_hook_petsc_style(cuda):
     """custom_solver plug-in (solver.py:278-280) written against the PETSc Mat interface of the
     documented example (A.getValuesCSR(), A.getSize(); scipy direct solve on the host) gives the
-    built-in solve's solution on the cube case (1e-10)."""
+    built-in solve's solution on the cube case (1e-9 of max|u|; both stop at Newton rel 1e-10)."""
     import scipy.sparse
     import scipy.sparse.linalg
     import jax_fem_gb300 as jf
@@ -437,7 +437,7 @@ def test_custom_solver_hook_petsc_style(cuda):
     ref = jf.solver(prob, {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-13},
                            "rel_tol": 1e-10, "tol": 0.0})[0]
     got = jf.solver(prob, {"custom_solver": host_direct, "rel_tol": 1e-10, "tol": 0.0})[0]
-    assert (got - ref).abs().max().item() <= 1e-10 * ref.abs().max().item()
+    assert (got - ref).abs().max().item() <= 1e-9 * ref.abs().max().item()
 
 
 def test_cube_gold_through_vtu_round_trip(cuda, tmp_path):
