@@ -164,13 +164,13 @@ def spmv_roofline(prob, peak):
     out = {}
     n, nnz, nnzb = eng.num_dofs, eng.nnz, eng.nnzb
     L_ = jf._lib
-    fmts = ((L_.FEM_SLICED_DF48, "df48", 6, 8, 8), (L_.FEM_SLICED_F32, "fp32", 4, 4, 4),
-            (L_.FEM_SLICED_F64, "fp64", 8, 8, 8))
+    fmts = ((L_.FEM_SYM_DF48, "sym_df48", 6, 8, 16), (L_.FEM_SLICED_DF48, "df48", 6, 8, 8),
+            (L_.FEM_SLICED_F32, "fp32", 4, 4, 4), (L_.FEM_SLICED_F64, "fp64", 8, 8, 8))
     for prec, name, es, xs, ys in fmts:
         A = eng._tangent_cache.get((prec, jf._lib.FEM_BC_SYMMETRIC))
         if A is None:
             continue
-        if prec == L_.FEM_SLICED_DF48:
+        if prec in (L_.FEM_SLICED_DF48, L_.FEM_SYM_DF48):
             pad = 4 if eng.vec == 3 else 1
             x = torch.zeros(eng.num_nodes, pad, 2, dtype=torch.float32, device="cuda")
             x[:, :eng.vec, 0] = torch.randn(eng.num_nodes, eng.vec, device="cuda")
@@ -181,8 +181,8 @@ def spmv_roofline(prob, peak):
             ws = torch.empty(nb.value, dtype=torch.uint8, device="cuda")
 
             def launch():
-                call("fem_spmv_dfx", C.byref(eng.pattern), eng.num_nodes, eng.vec, ptr(A.data), ptr(x), ptr(yh),
-                     ptr(yl), None, ptr(ws), nb.value, stream_handle())
+                call("fem_spmv_dfx", C.byref(eng.pattern), eng.num_nodes, eng.vec, prec, ptr(A.data), ptr(x),
+                     ptr(yh), ptr(yl), None, ptr(ws), nb.value, stream_handle())
         else:
             x = torch.randn(n, dtype=A.vector_dtype, device="cuda")
             y = torch.empty_like(x)
@@ -202,7 +202,13 @@ def spmv_roofline(prob, peak):
         ev[1].record(s)
         torch.cuda.synchronize()
         t = ev[0].elapsed_time(ev[1]) / 1e3 / reps
-        algo = nnz * es + nnzb * 4 + (eng.num_nodes + 1) * 8 + n * xs + n * ys
+        if prec == L_.FEM_SYM_DF48:
+            # the upper node blocks only; y is the double-float direct part plus the FP64
+            # transposed part (atomics), both written once per dof
+            nb_u = (nnzb - eng.num_nodes) // 2 + eng.num_nodes
+            algo = nb_u * eng.vec ** 2 * es + nb_u * 4 + (eng.n_slices + 1) * 8 + n * xs + n * ys
+        else:
+            algo = nnz * es + nnzb * 4 + (eng.num_nodes + 1) * 8 + n * xs + n * ys
         out[name] = {"seconds": t, "algorithmic_bytes": algo, "achieved_gbs": algo / t / 1e9,
                      "frac": algo / t / 1e9 / peak}
     return out
@@ -216,14 +222,18 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "spmv_sliced_dfdf_bulk_hex8_100x50x25.txt")
+TRAFFIC_PROFILES = {
+    "df48": os.path.join(ROOT, "profiles", "spmv_sliced_dfdf_bulk_hex8_100x50x25.txt"),
+    "sym_df48": os.path.join(ROOT, "profiles", "spmv_sym_df48_bulk_hex8_100x50x25.txt"),
+}
 
 
-def traffic_from_profile(n_units):
+def traffic_from_profile(n_units, kind="df48"):
     """DRAM bytes (read + write) per DF48 SpMV launch: the committed ncu summary's bytes per
-    nonzero on a smaller case, scaled to this workload's nnz (traffic grows with nnz)."""
+    nonzero (of the full matrix) on a smaller case, scaled to this workload's nnz (traffic grows
+    with nnz)."""
     try:
-        with open(TRAFFIC_PROFILE) as f:
+        with open(TRAFFIC_PROFILES[kind]) as f:
             for line in f:
                 if line.startswith("dram_bytes_per_nnz:"):
                     return float(line.split(":", 1)[1]) * n_units
@@ -553,8 +563,9 @@ def main():
         except Exception as exc:  # noqa: BLE001
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
 
-    f32 = roof.get("df48", roof.get("fp32", {}))
-    traffic = traffic_from_profile(nnz)
+    head = "sym_df48" if "sym_df48" in roof else "df48"
+    f32 = roof.get(head, roof.get("fp32", {}))
+    traffic = traffic_from_profile(nnz, head)
     value = job_seconds_per_iter(t_mx, args.steps, world)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -572,9 +583,15 @@ def main():
         "e2e": {"value": t_e2e / args.steps / world, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": f32.get("achieved_gbs"), "peak": peak, "unit": "GB/s",
                      "frac": f32.get("frac"), "traffic": traffic,
-                     "kernel": "spmv_sliced_dfdf_bulk_kernel<3> (fem_spmv_dfx: FEM_SLICED_DF48, bulk-copy staged, double-float on FP32 pipes)",
+                     "kernel": ("spmv_sliced_dfdf_bulk_kernel<3,SYM> (fem_spmv_dfx: FEM_SYM_DF48 upper node blocks, "
+                                "transposed half by FP64 atomics, bulk-copy staged, double-float on FP32 pipes; "
+                                "timed call includes the FP64 zero-fill and fold of the transposed half)"
+                                if head == "sym_df48" else
+                                "spmv_sliced_dfdf_bulk_kernel<3> (fem_spmv_dfx: FEM_SLICED_DF48, bulk-copy staged, "
+                                "double-float on FP32 pipes)"),
                      "peak_kind": peak_kind, "algorithmic_bytes": f32.get("algorithmic_bytes"),
-                     "launch_seconds": f32.get("seconds"), "fp64": roof.get("fp64"), "fp32": roof.get("fp32")},
+                     "launch_seconds": f32.get("seconds"), "fp64": roof.get("fp64"), "fp32": roof.get("fp32"),
+                     "sliced_df48": roof.get("df48") if head != "df48" else None},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "gpu_launches": int(launches),

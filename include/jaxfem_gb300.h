@@ -57,7 +57,13 @@ enum {
    * full coalesced line and no cross-lane reduction.  Vectors as for the unsliced type. */
   FEM_SLICED_F32 = 3,
   FEM_SLICED_F64 = 4,
-  FEM_SLICED_DF48 = 5
+  FEM_SLICED_DF48 = 5,
+  /* Symmetric sliced DF48: only the upper node blocks (block column >= row, diagonal first)
+   * of a symmetric matrix, in the sliced layout of fem_pattern_slices_upper (slice_ptr_u,
+   * slice_cols_u; padding slots point at the row itself with zero values).  The SpMV adds
+   * A_ij x_j to row i and A_ij^T x_i to row j (FP64 atomics into a separate FP64 vector),
+   * so it reads about half the bytes; its result is not bitwise reproducible. */
+  FEM_SYM_DF48 = 6
 };
 enum {                                                       /* built-in tensor maps     */
   FEM_MAT_LAPLACE = 1,        /* consts: [k]                      test_linear_poisson.py:15-17 */
@@ -99,6 +105,9 @@ typedef struct fem_pattern_t {
   int64_t n_slots;          /* total block slots of the sliced layout (host value)    */
   const int64_t* slice_ptr; /* (n_slices+1) first block slot of each 32-node slice    */
   const int32_t* slice_cols;/* (n_slots*32) block column of slot k, lane l (padding: 0) */
+  int64_t n_slots_u;        /* upper-block sliced layout (fem_pattern_slices_upper)  */
+  const int64_t* slice_ptr_u;
+  const int32_t* slice_cols_u;/* padding: the row's own node                         */
 } fem_pattern_t;
 
 typedef struct fem_material_t {
@@ -230,6 +239,10 @@ int fem_spmv(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t pre
  * n_slices = ceil(n_nodes/32)) and the slot count (host; syncs); otherwise fills slice_cols. */
 int fem_pattern_slices(int64_t n_nodes, const int64_t* block_ptr, const int32_t* block_cols,
                        int64_t* slice_ptr, int32_t* slice_cols, int64_t* n_slots, void* stream);
+/* The same for the upper node blocks of each row (block column >= row): slice_ptr_u,
+ * slice_cols_u and n_slots_u of the FEM_SYM_DF48 layout. */
+int fem_pattern_slices_upper(int64_t n_nodes, const int64_t* block_ptr, const int32_t* block_cols,
+                             int64_t* slice_ptr_u, int32_t* slice_cols_u, int64_t* n_slots_u, void* stream);
 /* Bytes of a value buffer for `pat` in `precision` (any FEM_F32 .. FEM_SLICED_DF48). */
 int fem_matrix_bytes(const fem_pattern_t* pat, int32_t vec, int32_t precision, size_t* bytes);
 /* FP64 CSR values -> values in `precision` (FEM_F32, FEM_DF48 or a sliced type). */
@@ -238,7 +251,8 @@ int fem_matrix_convert(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, c
 /* FP64 vector -> (hi[n], lo[n]) float pair, the FEM_DF48 SpMV input. */
 int fem_vector_split(const double* x, int64_t n, float* x_df, void* stream);
 /* The mixed CG's SpMV (no counterpart in the reference: the inner operator of
- * fem_pcg_refined with FEM_SLICED_DF48).  y = A x with A in FEM_SLICED_DF48; x is a
+ * fem_pcg_refined with FEM_SLICED_DF48 / FEM_SYM_DF48).  y = A x with A in `precision`
+ * (FEM_SLICED_DF48, or FEM_SYM_DF48 whose transposed half is folded into y); x is a
  * node-interleaved double-float vector: component c of node i is the float pair
  * (hi, lo) at pair index i*pad + c, pad = 4 for vec 3 (32 bytes per node) and 1 for vec 1;
  * y is written as y_hi[n] + y_lo[n] (scalar row order).  When xy_dot (device) is non-NULL it
@@ -246,8 +260,8 @@ int fem_vector_split(const double* x, int64_t n, float* x_df, void* stream);
  * For vec 3 with 16-byte aligned vals and slice_cols the slices are streamed through
  * shared memory by bulk copies (cp.async.bulk + mbarrier); a barrier wait that exceeds
  * its limit returns FEM_ERR_DEVICE. */
-int fem_spmv_dfx(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, const void* vals, const void* x_df,
-                 float* y_hi, float* y_lo, double* xy_dot, void* ws, size_t ws_bytes, void* stream);
+int fem_spmv_dfx(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision, const void* vals,
+                 const void* x_df, float* y_hi, float* y_lo, double* xy_dot, void* ws, size_t ws_bytes, void* stream);
 /* Jacobi: pc = 1/diag (n_dofs values); block Jacobi: inverse node blocks (n_nodes*vec*vec). */
 int fem_precond_setup(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
                       const void* vals, int32_t pc_kind, void* pc, void* stream);

@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "libjaxfem_gb300.so")
 # ---- constants mirrored from the header --------------------------------------
 FEM_OK, FEM_ERR_ARG, FEM_ERR_CUDA, FEM_ERR_UNSUPPORTED, FEM_ERR_CAPACITY, FEM_ERR_DEVICE = range(6)
 FEM_HEX8, FEM_TET10, FEM_TET4 = 1, 2, 3
-FEM_F32, FEM_F64, FEM_DF48, FEM_SLICED_F32, FEM_SLICED_F64, FEM_SLICED_DF48 = range(6)
+FEM_F32, FEM_F64, FEM_DF48, FEM_SLICED_F32, FEM_SLICED_F64, FEM_SLICED_DF48, FEM_SYM_DF48 = range(7)
 (FEM_MAT_LAPLACE, FEM_MAT_LINEAR_ELASTIC, FEM_MAT_SIMP, FEM_MAT_GENERAL_LINEAR,
  FEM_MAT_NEO_HOOKEAN, FEM_MAT_J2) = range(1, 7)
 FEM_OUT_RESIDUAL, FEM_OUT_MATRIX, FEM_OUT_APPLY = 1, 2, 4
@@ -41,7 +41,8 @@ class FemPattern(C.Structure):
     _fields_ = [("nnzb", C.c_int64), ("block_ptr", C.c_void_p), ("block_cols", C.c_void_p),
                 ("indptr", C.c_void_p), ("diag", C.c_void_p), ("slots", C.c_void_p),
                 ("n_slices", C.c_int64), ("n_slots", C.c_int64), ("slice_ptr", C.c_void_p),
-                ("slice_cols", C.c_void_p)]
+                ("slice_cols", C.c_void_p), ("n_slots_u", C.c_int64), ("slice_ptr_u", C.c_void_p),
+                ("slice_cols_u", C.c_void_p)]
 
 
 class FemMaterial(C.Structure):
@@ -91,7 +92,8 @@ SIGNATURES = {
     "fem_matrix_bytes": ([PPAT, I32, I32, PSZ], C.c_int),
     "fem_matrix_convert": ([PPAT, I64, I32, P, I32, P, P], C.c_int),
     "fem_vector_split": ([P, I64, P, P], C.c_int),
-    "fem_spmv_dfx": ([PPAT, I64, I32, P, P, P, P, P, P, SZ, P], C.c_int),
+    "fem_spmv_dfx": ([PPAT, I64, I32, I32, P, P, P, P, P, P, SZ, P], C.c_int),
+    "fem_pattern_slices_upper": ([I64, P, P, P, P, PI64, P], C.c_int),
     "fem_cast_f64_f32": ([P, P, I64, P, P], C.c_int),
     "fem_axpy_f32_f64": ([F64, P, P, I64, P], C.c_int),
     "fem_dot": ([I32, P, P, I64, P, P, SZ, P], C.c_int),

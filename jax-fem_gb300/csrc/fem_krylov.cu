@@ -36,8 +36,8 @@ struct KCtl {
   unsigned int ticket[4];
 };
 
-static bool is_sliced(int p) { return p == FEM_SLICED_F32 || p == FEM_SLICED_F64 || p == FEM_SLICED_DF48; }
-static bool is_df(int p) { return p == FEM_DF48 || p == FEM_SLICED_DF48; }
+static bool is_sliced(int p) { return p == FEM_SLICED_F32 || p == FEM_SLICED_F64 || p == FEM_SLICED_DF48 || p == FEM_SYM_DF48; }
+static bool is_df(int p) { return p == FEM_DF48 || p == FEM_SLICED_DF48 || p == FEM_SYM_DF48; }
 // FP32 vectors for FP32 matrices, FP64 vectors otherwise
 static bool vec_f32(int p) { return p == FEM_F32 || p == FEM_SLICED_F32; }
 
@@ -591,12 +591,17 @@ struct BulkGeom {
 
 // Sliced DF48 SpMV, bulk-copy staged: same arithmetic and outputs as spmv_sliced_dfdf_kernel.
 // Requires 16-byte aligned vals, vlo and slice_cols (checked by the host launcher).
-template <int VEC>
+// SYM: the matrix holds the upper node blocks only (FEM_SYM_DF48, diagonal block first in each
+// row); row i accumulates A_ij x_j in double-float as before and, for j != i, adds A_ij^T x_i to
+// row j through FP64 atomics into qT (zeroed by the caller, combined by the consumer).  The
+// fused dot is x.(A x) = sum_i 2 x_i.(sum_j A_ij x_j) - x_i.A_ii x_i.
+template <int VEC, bool SYM = false>
 __global__ void __launch_bounds__(BULK_WARPS * 32)
 spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* __restrict__ sp,
                              const int32_t* __restrict__ scols, const float* __restrict__ vals,
                              const int16_t* __restrict__ vlo, const float2* __restrict__ xp,
-                             float* __restrict__ yh, float* __restrict__ yl, KCtl* C, int op, double* partials) {
+                             float* __restrict__ yh, float* __restrict__ yl, KCtl* C, int op, double* partials,
+                             double* __restrict__ qT = nullptr) {
   using G = BulkGeom<VEC>;
   constexpr int VV = VEC * VEC;
   constexpr int PAD = DfNode<VEC>::PAD;
@@ -643,12 +648,28 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
 
   bool fault = false;
   float ds = 0.f, de = 0.f;
+  float dd_h = 0.f, dd_l = 0.f;   // SYM: sum of x_i.A_ii x_i
   int stage = 0;
   int64_t cs = warp, ck = 0, ce = 0;
   if (cs < n_slices) { ck = sp[cs]; ce = sp[cs + 1]; }
   float sh[VEC], sl[VEC];
 #pragma unroll
   for (int r = 0; r < VEC; ++r) { sh[r] = 0.f; sl[r] = 0.f; }
+  float xih[VEC], xil[VEC];       // SYM: the row's own x
+  bool first = true;              // SYM: next slot is the diagonal block
+  auto load_own = [&]() {
+    if constexpr (SYM) {
+      const int64_t i = cs * 32 + lane;
+      if (cs < n_slices && i < n_nodes) {
+        df_gather<VEC>(xp, i, xih, xil);
+      } else {
+#pragma unroll
+        for (int r = 0; r < VEC; ++r) { xih[r] = 0.f; xil[r] = 0.f; }
+      }
+      first = true;
+    }
+  };
+  load_own();
   while (cs < n_slices) {
     if (ck < ce) {
       const bool ok = mbar_wait(bars + stage, (parity >> stage) & 1u);
@@ -667,12 +688,49 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
 #pragma unroll
       for (int t = 0; t < BULK_SLOTS; ++t) {
         if (t < cnt) {
+          if constexpr (SYM) {
+            float ah[VV], al[VV];
 #pragma unroll
-          for (int v = 0; v < VV; ++v) {
-            const int r = v / VEC, d = v % VEC;
-            const float ah = sv[(t * VV + v) * 32 + lane];
-            const float al = df48_lo(ah, sq[(t * VV + v) * 32 + lane]);
-            df_acc(sh[r], sl[r], df2{ah, al}, df2{xvh[t][d], xvl[t][d]});
+            for (int v = 0; v < VV; ++v) {
+              ah[v] = sv[(t * VV + v) * 32 + lane];
+              al[v] = df48_lo(ah[v], sq[(t * VV + v) * 32 + lane]);
+            }
+            if (first) {  // diagonal block: A_ii x_i starts the row and its x.A x term
+#pragma unroll
+              for (int v = 0; v < VV; ++v) {
+                const int r = v / VEC, d = v % VEC;
+                df_acc(sh[r], sl[r], df2{ah[v], al[v]}, df2{xvh[t][d], xvl[t][d]});
+              }
+#pragma unroll
+              for (int r = 0; r < VEC; ++r) df_acc(dd_h, dd_l, df2{xih[r], xil[r]}, df_fast(sh[r], sl[r]));
+              first = false;
+            } else {
+#pragma unroll
+              for (int v = 0; v < VV; ++v) {
+                const int r = v / VEC, d = v % VEC;
+                df_acc(sh[r], sl[r], df2{ah[v], al[v]}, df2{xvh[t][d], xvl[t][d]});
+              }
+              const int j = sc[t * 32 + lane];
+              const int64_t i = cs * 32 + lane;
+              if (i < n_nodes && j != (int)i) {
+#pragma unroll
+                for (int d = 0; d < VEC; ++d) {
+                  float th = 0.f, tl = 0.f;
+#pragma unroll
+                  for (int r = 0; r < VEC; ++r)
+                    df_acc(th, tl, df2{ah[r * VEC + d], al[r * VEC + d]}, df2{xih[r], xil[r]});
+                  atomicAdd(qT + (int64_t)d * n_nodes + j, (double)th + (double)tl);   // component-major
+                }
+              }
+            }
+          } else {
+#pragma unroll
+            for (int v = 0; v < VV; ++v) {
+              const int r = v / VEC, d = v % VEC;
+              const float ah = sv[(t * VV + v) * 32 + lane];
+              const float al = df48_lo(ah, sq[(t * VV + v) * 32 + lane]);
+              df_acc(sh[r], sl[r], df2{ah, al}, df2{xvh[t][d], xvl[t][d]});
+            }
           }
         }
       }
@@ -698,6 +756,7 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
       for (int r = 0; r < VEC; ++r) { sh[r] = 0.f; sl[r] = 0.f; }
       cs += nwarps;
       if (cs < n_slices) { ck = sp[cs]; ce = sp[cs + 1]; }
+      load_own();
     }
   }
   if (fault) {
@@ -713,7 +772,23 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
     }
   }
   double dv[3] = {(double)ds + (double)de, 0.0, 0.0};
+  if constexpr (SYM) dv[0] = 2.0 * dv[0] - ((double)dd_h + (double)dd_l);
   reduce_and_finalize<1>(dv, C, op, partials, C->ticket, &C->d0);
+}
+
+// y (df) += qT (FP64, component-major: component c of node i at c * n_nodes + i), qT = 0: the
+// FEM_SYM_DF48 SpMV's transposed part folded into its result (vec 3)
+__global__ void sym_combine_kernel(int64_t n_nodes, float* __restrict__ yh, float* __restrict__ yl,
+                                   double* __restrict__ qT) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < 3 * n_nodes;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = k / 3;
+    const int64_t t = (k - 3 * i) * n_nodes + i;
+    const df2 y = df_add(df2{yh[k], yl[k]}, df_of(qT[t]));
+    yh[k] = y.h;
+    yl[k] = y.l;
+    qT[t] = 0.0;
+  }
 }
 
 // FP64 CSR values -> sliced layout (FP64, FP32 or DF48 hi/lo), thread per (slice, lane).
@@ -749,6 +824,40 @@ __global__ void to_sliced_kernel(int64_t n_nodes, int64_t n_slices, const int64_
           static_cast<float*>(out)[o] = h;
           lo[o] = (int16_t)q;
         }
+      }
+    }
+  }
+}
+
+// FP64 CSR values -> FEM_SYM_DF48 (the upper node blocks of each row), thread per (slice, lane).
+template <int VEC>
+__global__ void to_sliced_upper_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* bp, const int32_t* bcols,
+                                       const int64_t* sp, const double* v64, float* hi, int16_t* lo) {
+  constexpr int VV = VEC * VEC;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_slices * 32; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = t >> 5;
+    const int l = (int)(t & 31);
+    const int64_t i = s * 32 + l;
+    const int64_t b0 = i < n_nodes ? bp[i] : 0;
+    const int nb = i < n_nodes ? (int)(bp[i + 1] - b0) : 0;
+    int u0 = 0;
+    while (u0 < nb && bcols[b0 + u0] < i) ++u0;
+    const int64_t w = sp[s + 1] - sp[s];
+    for (int64_t k = 0; k < w; ++k) {
+      for (int v = 0; v < VV; ++v) {
+        const int r = v / VEC, d = v % VEC;
+        const double a = u0 + k < nb ? v64[(int64_t)VV * b0 + (int64_t)r * VEC * nb + VEC * (u0 + k) + d] : 0.0;
+        const int64_t o = ((sp[s] + k) * VV + v) * 32 + l;
+        const float h = __double2float_rn(a);
+        const int e = (__float_as_int(h) >> 23) & 0xFF;
+        int q = 0;
+        if (e > 39 && e < 255) {
+          double tq = rint(scalbn(a - (double)h, 166 - e));
+          tq = fmin(fmax(tq, -32767.0), 32767.0);
+          q = (int)tq;
+        }
+        hi[o] = h;
+        lo[o] = (int16_t)q;
       }
     }
   }
@@ -1046,12 +1155,12 @@ __global__ void pcgx_update_kernel(int64_t n_nodes, float* xh, float* xl, float*
 // the preconditioner blocks in nine, and the node-wise z = M r.h regroups through shared memory
 // (strides 3 and 9 are bank-conflict free).
 constexpr int VTILE_WARPS = VTHREADS / 32;
-template <int PC>
+template <int PC, bool SYM = false>
 __global__ void __launch_bounds__(VTHREADS)
 pcgx_update_tile_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restrict__ xl, float* __restrict__ rh,
                         float* __restrict__ rl, float* __restrict__ z, const float2* __restrict__ pp,
                         const float* __restrict__ qh, const float* __restrict__ ql, const float* __restrict__ pc,
-                        KCtl* C, double* partials, int op) {
+                        KCtl* C, double* partials, int op, double* __restrict__ qT) {
   constexpr int PCW = PC == FEM_PC_BJACOBI ? 9 : PC == FEM_PC_JACOBI ? 3 : 0;
   __shared__ float s_r[VTILE_WARPS][96], s_rl[VTILE_WARPS][96], s_z[VTILE_WARPS][96];
   __shared__ float s_pc[VTILE_WARPS][PCW > 0 ? 32 * PCW : 1];
@@ -1086,7 +1195,13 @@ pcgx_update_tile_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
         const df2 x = df_add(df2{xh[k], xl[k]}, df_mul(a, df2{pv.x, pv.y}));
         xh[k] = x.h;
         xl[k] = x.l;
-        const df2 r = df_add(df2{rh[k], rl[k]}, df_mul(na, df2{qh[k], ql[k]}));
+        df2 qv{qh[k], ql[k]};
+        if constexpr (SYM) {   // q = direct part (df) + transposed part (FP64, component-major), consumed here
+          const int64_t t = (int64_t)c * n_nodes + node0 + nl;
+          qv = df_add(qv, df_of(qT[t]));
+          qT[t] = 0.0;
+        }
+        const df2 r = df_add(df2{rh[k], rl[k]}, df_mul(na, qv));
         rh[k] = r.h;
         rl[k] = r.l;
         sr[o] = r.h;
@@ -1358,9 +1473,12 @@ struct KWs {
   size_t vec_bytes;
 };
 
+// 8 vectors of n_dofs elements plus 4 KB of alignment slack: the double-float CG carves 7 float
+// vectors, a node-interleaved direction (<= 11 bytes per dof) and 3 double vectors from the
+// FP64 size, i.e. <= 63 n bytes plus 256-byte rounding of each of its 11 arrays.
 static size_t krylov_ws_bytes(int64_t n_dofs, int precision) {
   const size_t es = precision == FEM_F32 ? 4 : 8;
-  return al(sizeof(KCtl)) + al(sizeof(double) * 3 * MAX_PARTIAL_BLOCKS) + 8 * al(es * (size_t)n_dofs);
+  return al(sizeof(KCtl)) + al(sizeof(double) * 3 * MAX_PARTIAL_BLOCKS) + 8 * al(es * (size_t)n_dofs) + 4096;
 }
 
 static KWs carve(void* ws, int64_t n_dofs, int precision) {
@@ -1468,12 +1586,18 @@ static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
 // The mixed CG's SpMV: bulk-copy staged kernel for vec 3 when the streamed arrays are 16-byte
 // aligned, the register-streaming kernel otherwise.  Grid: resident CTAs, capped by the slices.
-template <int VEC>
-static void launch_dfdf(const fem_pattern_t* pat, int64_t n_nodes, const float* vhi, const int16_t* vlo,
-                        const float2* xp, float* yh, float* yl, KCtl* C, int op, double* partials, cudaStream_t s) {
+// SYM (FEM_SYM_DF48, vec 3 only): the upper-block layout, transposed part into qT.
+template <int VEC, bool SYM = false>
+static int launch_dfdf(const fem_pattern_t* pat, int64_t n_nodes, const float* vhi, const int16_t* vlo,
+                       const float2* xp, float* yh, float* yl, KCtl* C, int op, double* partials, cudaStream_t s,
+                       double* qT = nullptr) {
   const int64_t ns = pat->n_slices;
-  if (VEC == 3 && aligned16(vhi) && aligned16(vlo) && aligned16(pat->slice_cols)) {
-    auto kern = spmv_sliced_dfdf_bulk_kernel<VEC>;
+  const int64_t* sp = SYM ? pat->slice_ptr_u : pat->slice_ptr;
+  const int32_t* sc = SYM ? pat->slice_cols_u : pat->slice_cols;
+  const bool bulk = VEC == 3 && aligned16(vhi) && aligned16(vlo) && aligned16(sc);
+  if (SYM && !(bulk && qT)) return fail(FEM_ERR_ARG, "FEM_SYM_DF48 needs vec 3 and 16-byte aligned arrays");
+  if (bulk) {
+    auto kern = spmv_sliced_dfdf_bulk_kernel<VEC, SYM>;
     constexpr int smem = (int)BulkGeom<VEC>::SMEM;
     static int per_sm = 0;
     if (per_sm == 0) {
@@ -1487,8 +1611,7 @@ static void launch_dfdf(const fem_pattern_t* pat, int64_t n_nodes, const float* 
     if (g > need) g = need;
     if (g > MAX_PARTIAL_BLOCKS) g = MAX_PARTIAL_BLOCKS;
     if (g < 1) g = 1;
-    kern<<<(unsigned)g, BULK_WARPS * 32, smem, s>>>(n_nodes, ns, pat->slice_ptr, pat->slice_cols, vhi, vlo, xp, yh,
-                                                    yl, C, op, partials);
+    kern<<<(unsigned)g, BULK_WARPS * 32, smem, s>>>(n_nodes, ns, sp, sc, vhi, vlo, xp, yh, yl, C, op, partials, qT);
   } else {
     auto kern = spmv_sliced_dfdf_kernel<VEC>;
     static int per_sm = 0;
@@ -1498,10 +1621,10 @@ static void launch_dfdf(const fem_pattern_t* pat, int64_t n_nodes, const float* 
     if (g > need) g = need;
     if (g > MAX_PARTIAL_BLOCKS) g = MAX_PARTIAL_BLOCKS;
     if (g < 1) g = 1;
-    kern<<<(unsigned)g, SPMV_THREADS, 0, s>>>(n_nodes, ns, pat->slice_ptr, pat->slice_cols, vhi, vlo, xp, yh, yl, C,
-                                              op, partials);
+    kern<<<(unsigned)g, SPMV_THREADS, 0, s>>>(n_nodes, ns, sp, sc, vhi, vlo, xp, yh, yl, C, op, partials);
   }
   note_launches(1);
+  return FEM_OK;
 }
 
 template <int VEC, typename T, int PC>
@@ -1719,6 +1842,7 @@ static inline size_t df_lo_offset(int64_t nnz) { return al(sizeof(float) * (size
 
 // Number of stored values of a matrix in `mfmt` (sliced layouts include their padding).
 static inline int64_t n_values(const fem_pattern_t* pat, int vec, int mfmt) {
+  if (mfmt == FEM_SYM_DF48) return pat->n_slots_u * vec * vec * 32;
   if (mfmt >= FEM_SLICED_F32) return pat->n_slots * vec * vec * 32;
   return pat->nnzb * vec * vec;
 }
@@ -1731,13 +1855,13 @@ static inline int64_t n_values(const fem_pattern_t* pat, int vec, int mfmt) {
 // as float pairs (FP32 pipes only); the FP64 true residual b - K x (matrix-free tangent
 // action) replaces r whenever the recursive residual has fallen by `delta`, and is the
 // only convergence test.  x (FP64, caller's buffer) is read at start and written back.
-template <int VEC, int PC>
+template <int VEC, int PC, bool SYM = false>
 static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* vals, const float* pc, const RefOp& op,
                         const double* b, double* x, double rtol, double atol, double delta, int64_t maxiter,
                         void* ws, int64_t* iters, int64_t* updates, double* rnorm, int32_t* status, cudaStream_t s) {
   const uint8_t* bc = op.bc;
   const int64_t n = n_nodes * VEC;
-  const int64_t m = n_values(pat, VEC, FEM_SLICED_DF48);
+  const int64_t m = n_values(pat, VEC, SYM ? FEM_SYM_DF48 : FEM_SLICED_DF48);
   const float* vhi = static_cast<const float*>(vals);
   const int16_t* vlo = reinterpret_cast<const int16_t*>(static_cast<const char*>(vals) + df_lo_offset(m));
   KWs w = carve(ws, n, FEM_F64);
@@ -1752,13 +1876,15 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
   float* qh = reinterpret_cast<float*>(v); v += f4;
   float* ql = reinterpret_cast<float*>(v); v += f4;
   double* ax = reinterpret_cast<double*>(v); v += d8;
-  double* r64 = reinterpret_cast<double*>(v);
+  double* r64 = reinterpret_cast<double*>(v); v += d8;
+  double* qT = SYM ? reinterpret_cast<double*>(v) : nullptr;   // transposed part of the SYM SpMV
+  if (SYM) FEM_CUDA(cudaMemsetAsync(qT, 0, sizeof(double) * (size_t)n, s));
   KCtl* C = w.ctl;
   const int gv = vec_grid(n), gn = vec_grid(n_nodes);
   // tile kernel: one warp per 32-node tile, grid = resident CTAs (no partial second wave)
   static int tile_per_sm = 0;
   if (tile_per_sm == 0 &&
-      (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tile_per_sm, pcgx_update_tile_kernel<PC>, VTHREADS, 0) !=
+      (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tile_per_sm, pcgx_update_tile_kernel<PC, SYM>, VTHREADS, 0) !=
            cudaSuccess ||
        tile_per_sm < 1))
     tile_per_sm = 1;
@@ -1821,10 +1947,11 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
       }
       if (launched >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
       for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
-        launch_dfdf<VEC>(pat, n_nodes, vhi, vlo, pp, qh, ql, C, FIN_PCG_ALPHA, w.partials, s);
+        rc = launch_dfdf<VEC, SYM>(pat, n_nodes, vhi, vlo, pp, qh, ql, C, FIN_PCG_ALPHA, w.partials, s, qT);
+        if (rc) return rc;
         if constexpr (VEC == 3) {
-          pcgx_update_tile_kernel<PC><<<gt, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
-                                                              w.partials, FIN_PCGR_UPDATE);
+          pcgx_update_tile_kernel<PC, SYM><<<gt, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
+                                                                   w.partials, FIN_PCGR_UPDATE, qT);
           pcgx_direction3_kernel<<<gv, VTHREADS, 0, s>>>(n, z, pp, C);
         } else {
           pcgx_update_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
@@ -1942,9 +2069,11 @@ static int check_pat(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int
   FEM_REQUIRE(pat && pat->block_ptr && pat->block_cols, "pattern NULL");
   FEM_REQUIRE(n_nodes > 0, "n_nodes must be positive");
   FEM_REQUIRE(vec == 1 || vec == 3, "vec must be 1 or 3");
-  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SLICED_DF48, "bad precision");
+  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SYM_DF48, "bad precision");
   FEM_REQUIRE(!is_sliced(precision) || (pat->n_slices == (n_nodes + 31) / 32 && pat->slice_ptr && pat->slice_cols),
               "sliced format needs the pattern's slice arrays (fem_pattern_slices)");
+  FEM_REQUIRE(precision != FEM_SYM_DF48 || (pat->slice_ptr_u && pat->slice_cols_u && pat->n_slots_u > 0),
+              "FEM_SYM_DF48 needs the upper-block slice arrays (fem_pattern_slices_upper)");
   return FEM_OK;
 }
 
@@ -1952,6 +2081,7 @@ extern "C" int fem_spmv(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, 
                         const void* x, void* y, void* stream) {
   int rc = check_pat(pat, n_nodes, vec, precision);
   if (rc) return rc;
+  FEM_REQUIRE(precision != FEM_SYM_DF48, "FEM_SYM_DF48 matrices are applied by fem_spmv_dfx");
   FEM_REQUIRE(vals && x && y, "NULL vector");
   cudaStream_t s = as_stream(stream);
   if (is_df(precision)) {
@@ -2025,7 +2155,7 @@ extern "C" int fem_precond_setup(const fem_pattern_t* pat, int64_t n_nodes, int3
 
 extern "C" int fem_krylov_workspace(int64_t n_dofs, int32_t precision, size_t* bytes) {
   FEM_REQUIRE(bytes && n_dofs >= 0, "bad arguments");
-  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SLICED_DF48, "bad precision");
+  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SYM_DF48, "bad precision");
   *bytes = krylov_ws_bytes(n_dofs, vec_f32(precision) ? FEM_F32 : FEM_F64);
   return FEM_OK;
 }
@@ -2146,7 +2276,10 @@ extern "C" int fem_pcg_refined(const fem_pattern_t* pat, int64_t n_nodes, int32_
   const float* P = (const float*)pc32;
 #define FEM_REF_CASE(VEC, PC)                                                                                   \
   if (vec == VEC && pc_kind == PC)                                                                              \
-    return precision == FEM_SLICED_DF48                                                                         \
+    return precision == FEM_SYM_DF48                                                                            \
+               ? pcg_dfx_impl<VEC, PC, true>(pat, n_nodes, vals32, P, op, b, x, rtol, atol, delta, maxiter, ws, \
+                                             iterations, updates, res_norm, status, s)                         \
+           : precision == FEM_SLICED_DF48                                                                       \
                ? pcg_dfx_impl<VEC, PC>(pat, n_nodes, vals32, P, op, b, x, rtol, atol, delta, maxiter, ws,       \
                                        iterations, updates, res_norm, status, s)                               \
            : is_df(precision)                                                                                   \
@@ -2166,8 +2299,9 @@ extern "C" int fem_pcg_refined(const fem_pattern_t* pat, int64_t n_nodes, int32_
 
 extern "C" int fem_matrix_bytes(const fem_pattern_t* pat, int32_t vec, int32_t precision, size_t* bytes) {
   FEM_REQUIRE(pat && bytes && (vec == 1 || vec == 3), "bad arguments");
-  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SLICED_DF48, "bad precision");
+  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SYM_DF48, "bad precision");
   FEM_REQUIRE(!is_sliced(precision) || pat->n_slices > 0, "sliced format needs fem_pattern_slices first");
+  FEM_REQUIRE(precision != FEM_SYM_DF48 || pat->n_slots_u > 0, "FEM_SYM_DF48 needs fem_pattern_slices_upper first");
   const int64_t m = n_values(pat, vec, precision);
   if (is_df(precision)) *bytes = df_lo_offset(m) + sizeof(int16_t) * (size_t)m;
   else if (vec_f32(precision)) *bytes = sizeof(float) * (size_t)m;
@@ -2183,7 +2317,13 @@ extern "C" int fem_matrix_convert(const fem_pattern_t* pat, int64_t n_nodes, int
   FEM_REQUIRE(precision != FEM_F64, "FP64 CSR values need no conversion");
   cudaStream_t s = as_stream(stream);
   const int64_t nnz = pat->nnzb * vec * vec;
-  if (precision == FEM_DF48) {
+  if (precision == FEM_SYM_DF48) {
+    FEM_REQUIRE(vec == 3, "FEM_SYM_DF48 is built for vec 3");
+    const int64_t m = n_values(pat, vec, precision);
+    int16_t* lo = reinterpret_cast<int16_t*>((char*)out + df_lo_offset(m));
+    to_sliced_upper_kernel<3><<<grid_for(pat->n_slices * 32, 256), 256, 0, s>>>(
+        n_nodes, pat->n_slices, pat->block_ptr, pat->block_cols, pat->slice_ptr_u, vals64, (float*)out, lo);
+  } else if (precision == FEM_DF48) {
     float* hi = (float*)out;
     int16_t* lo = reinterpret_cast<int16_t*>((char*)out + df_lo_offset(nnz));
     split_df_kernel<<<grid_for(nnz, 256), 256, 0, s>>>(vals64, nnz, hi, lo);
@@ -2219,24 +2359,37 @@ extern "C" int fem_vector_split(const double* x, int64_t n, float* x_df, void* s
   return check_launch("split_vec");
 }
 
-extern "C" int fem_spmv_dfx(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, const void* vals,
-                            const void* x_df, float* y_hi, float* y_lo, double* xy_dot, void* ws, size_t ws_bytes,
-                            void* stream) {
+extern "C" int fem_spmv_dfx(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
+                            const void* vals, const void* x_df, float* y_hi, float* y_lo, double* xy_dot, void* ws,
+                            size_t ws_bytes, void* stream) {
   FEM_REQUIRE(pat && vals && x_df && y_hi && y_lo && ws, "NULL argument");
-  FEM_REQUIRE(vec == 1 || vec == 3, "vec must be 1 or 3");
-  FEM_REQUIRE(pat->n_slices > 0 && pat->slice_ptr && pat->slice_cols, "pattern has no sliced layout");
+  FEM_REQUIRE(precision == FEM_SLICED_DF48 || precision == FEM_SYM_DF48, "precision must be a sliced DF48 type");
+  int rc0 = check_pat(pat, n_nodes, vec, precision);
+  if (rc0) return rc0;
   FEM_REQUIRE(ws_bytes >= krylov_ws_bytes(n_nodes * vec, FEM_F64), "workspace too small");
   cudaStream_t s = as_stream(stream);
-  const int64_t m = n_values(pat, vec, FEM_SLICED_DF48);
+  const int64_t m = n_values(pat, vec, precision);
   const float* vhi = static_cast<const float*>(vals);
   const int16_t* vlo = reinterpret_cast<const int16_t*>(static_cast<const char*>(vals) + df_lo_offset(m));
   KWs w = carve(ws, n_nodes * vec, FEM_F64);
   init_ctl_kernel<<<1, 32, 0, s>>>(w.ctl, 0.0, 0.0, 0);
   note_launches(1);
   const float2* xp = static_cast<const float2*>(x_df);
-  if (vec == 3) launch_dfdf<3>(pat, n_nodes, vhi, vlo, xp, y_hi, y_lo, w.ctl, FIN_DOT, w.partials, s);
-  else launch_dfdf<1>(pat, n_nodes, vhi, vlo, xp, y_hi, y_lo, w.ctl, FIN_DOT, w.partials, s);
-  int rc = check_launch("spmv_dfx");
+  int rc;
+  if (precision == FEM_SYM_DF48) {
+    double* qT = reinterpret_cast<double*>(w.vecs);
+    FEM_CUDA(cudaMemsetAsync(qT, 0, sizeof(double) * (size_t)(n_nodes * vec), s));
+    rc = launch_dfdf<3, true>(pat, n_nodes, vhi, vlo, xp, y_hi, y_lo, w.ctl, FIN_DOT, w.partials, s, qT);
+    if (rc) return rc;
+    sym_combine_kernel<<<vec_grid(n_nodes * vec), VTHREADS, 0, s>>>(n_nodes, y_hi, y_lo, qT);
+    note_launches(1);
+  } else if (vec == 3) {
+    rc = launch_dfdf<3>(pat, n_nodes, vhi, vlo, xp, y_hi, y_lo, w.ctl, FIN_DOT, w.partials, s);
+  } else {
+    rc = launch_dfdf<1>(pat, n_nodes, vhi, vlo, xp, y_hi, y_lo, w.ctl, FIN_DOT, w.partials, s);
+  }
+  if (rc) return rc;
+  rc = check_launch("spmv_dfx");
   if (rc) return rc;
   if (xy_dot) FEM_CUDA(cudaMemcpyAsync(xy_dot, &w.ctl->d0, sizeof(double), cudaMemcpyDeviceToDevice, s));
   return FEM_OK;

@@ -343,7 +343,69 @@ __global__ void slice_cols_kernel(int64_t n_nodes, int64_t n_slices, const int64
       scols[(sp[s] + k) * 32 + l] = k < nb ? bcols[b0 + k] : 0;
   }
 }
+// Upper node blocks of row i: the suffix of its sorted block columns starting at the first
+// column >= i (the diagonal).
+__device__ __forceinline__ int64_t first_upper(const int32_t* bcols, int64_t b0, int64_t nb, int64_t i) {
+  int64_t u = 0;
+  while (u < nb && bcols[b0 + u] < i) ++u;
+  return u;
+}
+
+__global__ void slice_width_upper_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* bp, const int32_t* bcols,
+                                         int64_t* widths) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n_slices; s += (int64_t)gridDim.x * blockDim.x) {
+    int64_t w = 0;
+    for (int l = 0; l < 32; ++l) {
+      const int64_t i = s * 32 + l;
+      if (i < n_nodes) {
+        const int64_t nb = bp[i + 1] - bp[i];
+        const int64_t nu = nb - first_upper(bcols, bp[i], nb, i);
+        w = nu > w ? nu : w;
+      }
+    }
+    widths[s] = w;
+  }
+}
+
+__global__ void slice_cols_upper_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* bp, const int32_t* bcols,
+                                        const int64_t* sp, int32_t* scols) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_slices * 32; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = t >> 5;
+    const int l = (int)(t & 31);
+    const int64_t i = s * 32 + l;
+    const int64_t b0 = i < n_nodes ? bp[i] : 0;
+    const int64_t nb = i < n_nodes ? bp[i + 1] - b0 : 0;
+    const int64_t u0 = i < n_nodes ? first_upper(bcols, b0, nb, i) : 0;
+    const int32_t pad = i < n_nodes ? (int32_t)i : 0;
+    for (int64_t k = 0; k < sp[s + 1] - sp[s]; ++k)
+      scols[(sp[s] + k) * 32 + l] = u0 + k < nb ? bcols[b0 + u0 + k] : pad;
+  }
+}
 }  // namespace fem
+
+extern "C" int fem_pattern_slices_upper(int64_t n_nodes, const int64_t* block_ptr, const int32_t* block_cols,
+                                        int64_t* slice_ptr_u, int32_t* slice_cols_u, int64_t* n_slots_u,
+                                        void* stream) {
+  FEM_REQUIRE(n_nodes > 0 && block_ptr && block_cols && slice_ptr_u, "bad arguments");
+  cudaStream_t s = as_stream(stream);
+  const int64_t n_slices = (n_nodes + 31) / 32;
+  if (slice_cols_u == nullptr) {
+    FEM_REQUIRE(n_slots_u, "n_slots_u NULL");
+    slice_width_upper_kernel<<<grid_for(n_slices, 256), 256, 0, s>>>(n_nodes, n_slices, block_ptr, block_cols,
+                                                                      slice_ptr_u);
+    scan_single_block<<<1, SCAN_THREADS, 0, s>>>(slice_ptr_u, n_slices);
+    note_launches(2);
+    int rc = check_launch("upper slice widths");
+    if (rc) return rc;
+    FEM_CUDA(cudaMemcpyAsync(n_slots_u, slice_ptr_u + n_slices, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    FEM_CUDA(cudaStreamSynchronize(s));
+    return FEM_OK;
+  }
+  slice_cols_upper_kernel<<<grid_for(n_slices * 32, 256), 256, 0, s>>>(n_nodes, n_slices, block_ptr, block_cols,
+                                                                        slice_ptr_u, slice_cols_u);
+  note_launches(1);
+  return check_launch("upper slice cols");
+}
 
 extern "C" int fem_pattern_slices(int64_t n_nodes, const int64_t* block_ptr, const int32_t* block_cols,
                                   int64_t* slice_ptr, int32_t* slice_cols, int64_t* n_slots, void* stream) {

@@ -50,6 +50,8 @@ class DeviceCSR:
         return self.eng.scalar_indices()
 
     def matvec(self, x):
+        if self.precision == _lib.FEM_SYM_DF48:
+            return self._matvec_dfx(x)
         if self.precision in (_lib.FEM_DF48, _lib.FEM_SLICED_DF48):
             x = x.to(torch.float64).contiguous()
             xs = torch.empty(2 * x.numel(), dtype=torch.float32, device=x.device)
@@ -63,6 +65,22 @@ class DeviceCSR:
         call("fem_spmv", C.byref(self.eng.pattern), self.eng.num_nodes, self.eng.vec, self.precision,
              ptr(self.data), ptr(x), ptr(y), _stream())
         return y
+
+    def _matvec_dfx(self, x):
+        """fem_spmv_dfx on a node-interleaved double-float copy of x (FP64 result)."""
+        eng = self.eng
+        x = x.to(torch.float64).reshape(-1)
+        pad = 4 if eng.vec == 3 else 1
+        hi = x.float()
+        xp = torch.zeros(eng.num_nodes, pad, 2, dtype=torch.float32, device=x.device)
+        xp[:, :eng.vec, 0] = hi.view(-1, eng.vec)
+        xp[:, :eng.vec, 1] = (x - hi.double()).float().view(-1, eng.vec)
+        yh = torch.empty(eng.num_dofs, dtype=torch.float32, device=x.device)
+        yl = torch.empty_like(yh)
+        ws = eng.workspace(_lib.FEM_SLICED_DF48)
+        call("fem_spmv_dfx", C.byref(eng.pattern), eng.num_nodes, eng.vec, self.precision, ptr(self.data), ptr(xp),
+             ptr(yh), ptr(yl), None, ptr(ws), ws.numel(), _stream())
+        return yh.double() + yl.double()
 
     __matmul__ = matvec
 
@@ -209,10 +227,19 @@ class Engine:
         self.slice_cols = torch.empty(self.n_slots * 32, dtype=torch.int32, device=dev)
         call("fem_pattern_slices", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols), ptr(self.slice_ptr),
              ptr(self.slice_cols), None, s)
+        # upper node blocks only: the symmetric DF48 solver copy (FEM_SYM_DF48)
+        self.slice_ptr_u = torch.empty(self.n_slices + 1, dtype=torch.int64, device=dev)
+        call("fem_pattern_slices_upper", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols),
+             ptr(self.slice_ptr_u), None, C.byref(n_slots), s)
+        self.n_slots_u = n_slots.value
+        self.slice_cols_u = torch.empty(self.n_slots_u * 32, dtype=torch.int32, device=dev)
+        call("fem_pattern_slices_upper", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols),
+             ptr(self.slice_ptr_u), ptr(self.slice_cols_u), None, s)
         self.pattern = _lib.FemPattern(self.nnzb, self.block_ptr.data_ptr(), self.block_cols.data_ptr(),
                                        self.indptr.data_ptr(), self.diag.data_ptr(), self.slots.data_ptr(),
                                        self.n_slices, self.n_slots, self.slice_ptr.data_ptr(),
-                                       self.slice_cols.data_ptr())
+                                       self.slice_cols.data_ptr(), self.n_slots_u, self.slice_ptr_u.data_ptr(),
+                                       self.slice_cols_u.data_ptr())
         self._indices = None
 
     def scalar_indices(self):

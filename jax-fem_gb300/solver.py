@@ -102,14 +102,22 @@ def resolve_linear(linear_options):
 
 def _precision(cfg):
     p = cfg.get("precision", "fp64")
-    if p not in ("fp64", "mixed", "mixed32"):
-        raise ValueError("precision must be 'fp64', 'mixed' (DF48 matrix, FP64 vectors) or 'mixed32' (FP32)")
+    if p not in ("fp64", "mixed", "mixed_sym", "mixed32"):
+        raise ValueError("precision must be 'fp64', 'mixed' (DF48 matrix, FP64 vectors), 'mixed_sym' (the same "
+                         "with upper-block DF48 storage) or 'mixed32' (FP32)")
     return p
 
 
-def _mixed_matrix_precision(precision):
-    """Solver copy of the tangent: sliced DF48 for 'mixed', sliced FP32 for 'mixed32'."""
-    return _lib.FEM_SLICED_DF48 if precision == "mixed" else _lib.FEM_SLICED_F32
+def _mixed_matrix_precision(precision, eng=None):
+    """Solver copy of the tangent: sliced DF48 for 'mixed'; the symmetric DF48 layout (upper node
+    blocks, transposed half through FP64 atomics) for 'mixed_sym' when the tangent is symmetric
+    and vec = 3 -- it reads about half the matrix bytes but is slower on GB300 (the FP64 atomics
+    cost more than the bytes saved); sliced FP32 for 'mixed32'."""
+    if precision == "mixed_sym" and eng is not None and eng.vec == 3 and getattr(eng._mat, "symmetric", False):
+        return _lib.FEM_SYM_DF48
+    if precision in ("mixed", "mixed_sym"):
+        return _lib.FEM_SLICED_DF48
+    return _lib.FEM_SLICED_F32
 
 
 _FP64_SOLVER_FORMAT = _lib.FEM_SLICED_F64     # FP64 Krylov iterations run on the sliced FP64 copy
@@ -152,8 +160,8 @@ def _timed(eng, key, t0):
 def _newton_step(problem, eng, dofs, res, spec, precision, cfg):
     """One Newton correction A inc = -res (solver.py:390-421) with the Dirichlet rows of the
     increment equal to g - u_b."""
-    prec = _FP64_SOLVER_FORMAT if precision == "fp64" else _mixed_matrix_precision(precision)
-    if prec == _lib.FEM_SLICED_DF48 and spec.method != "cg":
+    prec = _FP64_SOLVER_FORMAT if precision == "fp64" else _mixed_matrix_precision(precision, eng)
+    if prec in (_lib.FEM_SLICED_DF48, _lib.FEM_SYM_DF48) and spec.method != "cg":
         prec = _lib.FEM_SLICED_F32   # BiCGStab mixed path runs in FP32 with Newton-level refinement
     eng.refresh_bc()
     rows = eng.bc_rows_long
@@ -328,7 +336,7 @@ def adjoint_solve(problem, dofs, v, adjoint_solver_options=None, precision="fp64
         eng.krylov(spec.method, A, b, lam, spec.pc, spec.rtol, spec.atol, spec.maxiter)
         _timed(eng, "linear", t0)
         return lam
-    mprec = _mixed_matrix_precision(prec_opt) if spec.method == "cg" else _lib.FEM_SLICED_F32
+    mprec = _mixed_matrix_precision(prec_opt, eng) if spec.method == "cg" else _lib.FEM_SLICED_F32
     A = eng.tangent(dofs, mprec, _lib.FEM_BC_SYMMETRIC)
     lam = torch.zeros_like(b)
     if spec.method == "cg":

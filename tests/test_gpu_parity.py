@@ -235,14 +235,16 @@ def test_simp_adjoint_vs_oracle_and_fd(cuda):
         assert abs(fd - g[c, 0]) <= 1e-5 * np.abs(g).max()
 
 
-def test_mixed_precision_matches_fp64(cuda):
-    """Mixed (FP32 tangent + FP32 PCG in FP64 refinement) vs FP64: solution, objective, gradient."""
+@pytest.mark.parametrize("mode", ["mixed", "mixed_sym"])
+def test_mixed_precision_matches_fp64(cuda, mode):
+    """Mixed (DF48 matrix, double-float CG, FP64 reliable updates; with mixed_sym the upper-block
+    DF48 storage) vs FP64: solution, objective, gradient."""
     import cases
     prob, _, theta_np = cases.simp_box(12, 6, 3)
     o64 = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}, "rel_tol": 1e-12, "tol": 0.0}
-    omx = dict(o64, precision="mixed")
+    omx = dict(o64, precision=mode)
     a64 = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}}
-    amx = dict(a64, precision="mixed")
+    amx = dict(a64, precision=mode)
     s64, J64, g64 = _simp_grad(prob, theta_np, cuda, o64, a64)
     smx, Jmx, gmx = _simp_grad(prob, theta_np, cuda, omx, amx)
     assert (smx - s64).abs().max().item() <= 1e-9 * s64.abs().max().item()
@@ -356,7 +358,8 @@ def test_df48_spmv_matches_fp64(cuda):
     x = torch.randn(eng.num_dofs, dtype=torch.float64, device=cuda)
     y64 = A64.matvec(x)
     L = jf._lib
-    for fmt, tol in ((L.FEM_DF48, 1e-11), (L.FEM_SLICED_DF48, 1e-11), (L.FEM_SLICED_F64, 1e-14),
+    for fmt, tol in ((L.FEM_DF48, 1e-11), (L.FEM_SLICED_DF48, 1e-11), (L.FEM_SYM_DF48, 1e-11),
+                     (L.FEM_SLICED_F64, 1e-14),
                      (L.FEM_SLICED_F32, 1e-6)):
         A = eng.tangent(z, fmt, jf._lib.FEM_BC_SYMMETRIC, cache=False)
         y = A.matvec(x).double()
@@ -385,11 +388,14 @@ def _df_nodes(x, vec):
     return xp
 
 
+@pytest.mark.parametrize("sym", [False, True])
 @pytest.mark.parametrize("n", [(10, 5, 3), (64, 40, 40)])
-def test_spmv_dfx_matches_fp64(cuda, n):
+def test_spmv_dfx_matches_fp64(cuda, n, sym):
     """The mixed CG's SpMV (bulk-copy staged, double-float in and out) against the FP64 SpMV:
     y to 1e-11 of max|y|, the fused dot x.y to 1e-11 relative.  (64, 40, 40) has more slices
-    than resident warps, so warps stream several slices through their shared-memory ring."""
+    than resident warps, so warps stream several slices through their shared-memory ring.  With
+    sym the matrix is FEM_SYM_DF48 (upper node blocks; the transposed half through FP64 atomics,
+    the dot through x.Ax = 2 x.(upper part) - x.diag)."""
     import ctypes as C
     import jax_fem_gb300 as jf
     import cases
@@ -399,7 +405,8 @@ def test_spmv_dfx_matches_fp64(cuda, n):
     eng = prob._engine
     z = torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda)
     A64 = eng.tangent(z, L.FEM_F64, L.FEM_BC_SYMMETRIC, cache=False)
-    Adf = eng.tangent(z, L.FEM_SLICED_DF48, L.FEM_BC_SYMMETRIC, cache=False)
+    fmt = L.FEM_SYM_DF48 if sym else L.FEM_SLICED_DF48
+    Adf = eng.tangent(z, fmt, L.FEM_BC_SYMMETRIC, cache=False)
     g = torch.Generator(device=cuda).manual_seed(3)
     x = torch.randn(eng.num_dofs, dtype=torch.float64, device=cuda, generator=g)
     y64 = A64.matvec(x)
@@ -411,8 +418,8 @@ def test_spmv_dfx_matches_fp64(cuda, n):
     L.call("fem_krylov_workspace", eng.num_dofs, L.FEM_SLICED_DF48, C.byref(nb))
     ws = torch.empty(nb.value, dtype=torch.uint8, device=cuda)
     for _ in range(2):  # a second call reuses the workspace and its control block
-        L.call("fem_spmv_dfx", C.byref(eng.pattern), eng.num_nodes, 3, L.ptr(Adf.data), L.ptr(xp), L.ptr(yh),
-               L.ptr(yl), L.ptr(dot), L.ptr(ws), nb.value, L.stream_handle())
+        L.call("fem_spmv_dfx", C.byref(eng.pattern), eng.num_nodes, 3, fmt, L.ptr(Adf.data), L.ptr(xp),
+               L.ptr(yh), L.ptr(yl), L.ptr(dot), L.ptr(ws), nb.value, L.stream_handle())
         y = yh.double() + yl.double()
         assert (y - y64).abs().max().item() <= 1e-11 * y64.abs().max().item()
         ref = torch.dot(x, y64).item()
