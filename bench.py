@@ -362,6 +362,120 @@ def kernel_shares(args):
             print(f"{cnt[k]:9d} {v / 1e3:10.2f} {100 * v / T:6.2f}% {v / cnt[k]:10.2f}  {k}")
 
 
+def _neo_box(n, traction=None, stretch=None):
+    """Neo-Hookean (E=10, nu=0.3) unit cube, x=0 clamped; an end traction on x=1 or a stretch
+    u_x = stretch there.  Returns (GPU problem, oracle problem builder)."""
+    import torch
+    import jax_fem_gb300 as jf
+    m = jf.box_mesh(n, n, n, 1.0, 1.0, 1.0)
+    pts, cells = m.points, m.cells_dict["hexahedron"]
+    left = lambda p: np.isclose(p[0], 0.0, atol=1e-5)
+    right = lambda p: np.isclose(p[0], 1.0, atol=1e-5)
+    zero = lambda p: 0.0
+    if stretch is not None:
+        bc = [[left] * 3 + [right] * 3, [0, 1, 2, 0, 1, 2], [zero] * 3 + [lambda p: stretch, zero, zero]]
+    else:
+        bc = [[left] * 3, [0, 1, 2], [zero] * 3]
+    locs = [right] if traction is not None else None
+
+    class P(jf.Problem):
+        def get_tensor_map(self):
+            return jf.NeoHookean(10.0, 0.3)
+
+        if traction is not None:
+            def get_surface_maps(self):
+                return [lambda u, x: np.array(traction)]
+
+    def oracle():
+        from oracle import fem as ofem, materials as omat
+        return ofem.OracleProblem(pts, cells, 3, dirichlet_bc_info=bc, location_fns=locs,
+                                  tensor_map=omat.neo_hookean(10.0, 0.3),
+                                  surface_maps=None if traction is None else
+                                  [lambda u, x: torch.tensor(traction, dtype=torch.float64)])
+    return P(jf.Mesh(pts, cells), vec=3, dim=3, dirichlet_bc_info=bc, location_fns=locs), oracle
+
+
+def widened_bench(args):
+    """The nonlinear drivers and Robin maps beside the step: each solve timed end to end on the
+    GPU (CUDA-synchronised wall clock) and as the oracle port on the host, on the same small
+    case.  Prints one JSON line; not the headline metric."""
+    import torch
+    import jax_fem_gb300 as jf
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, out
+
+    rows = {}
+    # dynamic relaxation (solver.py:918-1049)
+    prob, oracle = _neo_box(10, traction=[0.0, 0.0, -0.2])
+    opts = {"dynamic_relax": {"tol": 1e-6, "nKMat": 50, "info": False, "info_force": False}}
+    jf.solver(prob, opts)
+    t_gpu, _ = timed(lambda: jf.solver(prob, opts))
+    rec = {"case": "Neo-Hookean HEX8 10^3, end traction, tol 1e-6", "gpu_s": t_gpu,
+           "iterations": prob.dr_info["iterations"]}
+    if not args.no_cpu:
+        from oracle import drivers as odr
+        op = oracle()
+        t0 = time.perf_counter()
+        _, it_o = odr.dynamic_relax(op, tol=1e-6, nKMat=50)
+        rec.update(cpu_s=time.perf_counter() - t0, cpu_iterations=it_o)
+    rows["dynamic_relax"] = rec
+    # arc length, displacement control (solver.py:559-634, 759-793)
+    prob, oracle = _neo_box(6, stretch=0.3)
+    opts = {"arc_length": {"control": "displacement", "Delta_l": 0.1, "return_info": True,
+                           "newton": {"rel_tol": 1e-10, "tol": 1e-10},
+                           "linear": {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}}}}
+    jf.solver(prob, opts)
+    t_gpu, (_, info) = timed(lambda: jf.solver(prob, opts))
+    rec = {"case": "Neo-Hookean HEX8 6^3, x=1 stretch 0.3, Delta_l 0.1", "gpu_s": t_gpu,
+           "steps": len(info["history"])}
+    if not args.no_cpu:
+        from oracle import drivers as odr
+        op = oracle()
+        t0 = time.perf_counter()
+        _, _, lams = odr.arc_length(op, "displacement", delta_l=0.1, psi=1.0)
+        rec.update(cpu_s=time.perf_counter() - t0, cpu_steps=len(lams))
+    rows["arc_length"] = rec
+    # u-dependent (Robin) surface map, Newton (problem.py:238-259)
+    m = jf.box_mesh(20, 20, 20, 1.0, 1.0, 1.0)
+    pts, cells = m.points, m.cells_dict["hexahedron"]
+    left = lambda p: np.isclose(p[0], 0.0, atol=1e-5)
+    right = lambda p: np.isclose(p[0], 1.0, atol=1e-5)
+
+    class R(jf.Problem):
+        def get_tensor_map(self):
+            return jf.Laplace()
+
+        def get_surface_maps(self):
+            return [lambda u, x: 5.0 * u ** 2]
+
+    prob = R(jf.Mesh(pts, cells), vec=1, dim=3, dirichlet_bc_info=[[left], [0], [lambda p: 1.0]],
+             location_fns=[right])
+    opts = {"petsc_solver": {"ksp_type": "cg", "pc_type": "jacobi", "rtol": 1e-12}, "rel_tol": 1e-10, "tol": 0.0}
+    jf.solver(prob, opts)
+    t_gpu, _ = timed(lambda: jf.solver(prob, opts))
+    rec = {"case": "Laplace HEX8 20^3, u=1 at x=0, Robin 5u^2 on x=1, Newton rel 1e-10", "gpu_s": t_gpu,
+           "newton_iterations": prob.newton_info["iterations"]}
+    if not args.no_cpu:
+        import torch as _t
+        from oracle import fem as ofem, materials as omat, solve as osolve
+        op = ofem.OracleProblem(pts, cells, 1, dirichlet_bc_info=[[left], [0], [lambda p: 1.0]],
+                                location_fns=[right], tensor_map=omat.laplace(),
+                                surface_maps=[lambda u, x: 5.0 * u ** 2])
+        t0 = time.perf_counter()
+        osolve.newton_solve(op, {"spsolve_solver": {}, "rel_tol": 1e-10, "tol": 0.0})
+        rec["cpu_s"] = time.perf_counter() - t0
+    rows["robin_newton"] = rec
+    line = {"metric": "nonlinear drivers and Robin maps, solve wall time (s)", "unit": "s",
+            "higher_is_better": False, "data": "synthetic", "rows": rows,
+            "cpu_kind": "port (oracle restatement on the host: torch.func element kernels, scipy direct solves)"}
+    print(json.dumps(line))
+
+
 def mma_update_bench(args):
     """TO update beside the step (jax_fem/mma.py): sensitivity filter + one MMA update for every
     cell of the workload as design variable (m = 1 volume constraint), GPU against the oracle's
@@ -453,6 +567,8 @@ def main():
     ap.add_argument("--size", type=int, nargs=3, default=list(DEFAULT_SIZE))
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--widened", action="store_true",
+                    help="time the arc-length / dynamic-relaxation drivers and a Robin Newton solve (GPU and CPU port)")
     ap.add_argument("--mma-update", action="store_true",
                     help="time the TO update (filter + MMA) beside the step and print its own JSON line")
     ap.add_argument("--kernel-shares", action="store_true",
@@ -463,6 +579,9 @@ def main():
         return
     if args.mma_update:
         mma_update_bench(args)
+        return
+    if args.widened:
+        widened_bench(args)
         return
 
     rank = int(os.environ.get("RANK", "0"))
