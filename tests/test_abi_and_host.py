@@ -47,6 +47,34 @@ def test_argument_errors_without_gpu(lib):
     assert lib.fem_version() >= 100
 
 
+def test_widened_entry_points_validate_arguments(lib):
+    """The MMA, filter, Robin, history-VJP and driver entry points reject bad arguments with
+    FEM_ERR_ARG before touching the device (no GPU needed)."""
+    import ctypes as C
+    import jax_fem_gb300 as jf
+    L = jf._lib
+    nb = C.c_size_t()
+    L.call("fem_mma_workspace", 1000, 1, C.byref(nb))
+    assert nb.value > 8 * 1000 * 17
+    assert lib.fem_mma_workspace(1000, 5, C.byref(nb)) == L.FEM_ERR_ARG          # m <= 4
+    assert lib.fem_mma_workspace(0, 1, C.byref(nb)) == L.FEM_ERR_ARG
+    f = C.c_double(0.0)
+    rc = lib.fem_mma_update(3, 4, 1, *([None] * 7), 0.1, None, C.byref(f), None, 1.0, C.byref(f), C.byref(f),
+                            C.byref(f), None, None, 0, None, None)
+    assert rc == L.FEM_ERR_ARG                                                  # n must exceed m
+    L.call("fem_filter_workspace", 100, C.byref(nb))
+    assert lib.fem_filter_build(100, None, 0.1, 20, None, None, None, None, 0, None) == L.FEM_ERR_ARG
+    assert lib.fem_filter_apply(100, 40, None, None, None, None, None, 1, 0, None, None) == L.FEM_ERR_ARG
+    assert lib.fem_dr_march(0, 1.0, None, None, None, None, None, None) == L.FEM_ERR_ARG
+    assert lib.fem_row_abs_sum(10, None, None, 1.0, None, None) == L.FEM_ERR_ARG
+    mesh = L.FemMesh(L.FEM_HEX8, 3, 8, 1, None, None)
+    assert lib.fem_surface_robin(C.byref(mesh), None, None, None, 0, 5, None, 1, L.FEM_F64, None, None, None, 0,
+                                 None, None, None, None) == L.FEM_ERR_ARG         # degree <= 4
+    assert lib.fem_j2_history_vjp(C.byref(mesh), None, None, None, None, None, None, None, None,
+                                  None) == L.FEM_ERR_ARG
+    assert "J2" in L.last_error() or "NULL" in L.last_error() or "mesh" in L.last_error()
+
+
 def test_element_tables_match_oracle(lib):
     from jax_fem_gb300 import basis
     from oracle import basis as ob
