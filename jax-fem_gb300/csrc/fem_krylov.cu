@@ -1155,8 +1155,11 @@ __global__ void pcgx_update_kernel(int64_t n_nodes, float* xh, float* xl, float*
 // the preconditioner blocks in nine, and the node-wise z = M r.h regroups through shared memory
 // (strides 3 and 9 are bank-conflict free).
 constexpr int VTILE_WARPS = VTHREADS / 32;
+#ifndef FEM_TILE_MIN_BLOCKS
+#define FEM_TILE_MIN_BLOCKS 6   // 40 registers, 48 resident warps per SM: more loads in flight
+#endif
 template <int PC, bool SYM = false>
-__global__ void __launch_bounds__(VTHREADS)
+__global__ void __launch_bounds__(VTHREADS, FEM_TILE_MIN_BLOCKS)
 pcgx_update_tile_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restrict__ xl, float* __restrict__ rh,
                         float* __restrict__ rl, float* __restrict__ z, const float2* __restrict__ pp,
                         const float* __restrict__ qh, const float* __restrict__ ql, const float* __restrict__ pc,
