@@ -690,10 +690,10 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_mx / args.steps * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 assembly; DF48 matrix (fp32 hi + int16 lo) with double-float SpMV on fp32 pipes; f64 vectors/dots",
+        "dtype": "f64 assembly; DF48 matrix (fp32 hi + int16 lo) with double-float SpMV on fp32 pipes; double-float (fp32 pair) CG vectors, f64 dot finish and reliable updates",
         "data": "synthetic",
         "config": {"workload": name, "precision": "mixed", "tolerance": RTOL,
-                   "solver": "block-Jacobi PCG, DF48 SpMV + FP64 vectors, FP64 reliable updates (true residual)",
+                   "solver": "block-Jacobi PCG, DF48 SpMV + double-float CG vectors, FP64 reliable updates (true residual)",
                    "l2": "inputs larger than L2 (the DF48 matrix alone is 1.5 GB > 129 MB)",
                    "replicas": "one independent problem per GPU (no data-path collective)"},
         "pcg_iterations": its_mx,

@@ -103,7 +103,7 @@ def resolve_linear(linear_options):
 def _precision(cfg):
     p = cfg.get("precision", "fp64")
     if p not in ("fp64", "mixed", "mixed_sym", "mixed32"):
-        raise ValueError("precision must be 'fp64', 'mixed' (DF48 matrix, FP64 vectors), 'mixed_sym' (the same "
+        raise ValueError("precision must be 'fp64', 'mixed' (DF48 matrix, double-float vectors), 'mixed_sym' (the same "
                          "with upper-block DF48 storage) or 'mixed32' (FP32)")
     return p
 
