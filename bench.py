@@ -350,16 +350,32 @@ def kernel_shares(args):
             run_steps(prob, fwd, theta_step(th0, 1))
             torch.cuda.synchronize()
         tot, cnt = collections.defaultdict(float), collections.Counter()
+        spans = []
         for e in p.events():
             if e.device_type == torch.autograd.DeviceType.CUDA:
                 k = e.name.split("(")[0]
                 tot[k] += getattr(e, "device_time_total", 0.0) or e.cuda_time_total
                 cnt[k] += 1
+                tr = getattr(e, "time_range", None)
+                if tr is not None and tr.end > tr.start:
+                    spans.append((tr.start, tr.end))
         T = sum(tot.values())
         print(f"{prec} step, {workload_name(n)[0]}: {T / 1e3:.1f} ms of kernel time, {sum(cnt.values())} launches")
         print(f"{'launches':>9} {'total_ms':>10} {'share':>7} {'us/launch':>10}  kernel")
         for k, v in sorted(tot.items(), key=lambda kv: -kv[1])[:16]:
             print(f"{cnt[k]:9d} {v / 1e3:10.2f} {100 * v / T:6.2f}% {v / cnt[k]:10.2f}  {k}")
+        if len(spans) > 1:   # device idle between consecutive device activities, by gap size
+            spans.sort()
+            gaps, end = [], spans[0][1]
+            for a, b in spans[1:]:
+                if a > end:
+                    gaps.append(a - end)
+                end = max(end, b)
+            g = np.asarray(gaps) if gaps else np.zeros(1)
+            print(f"device span {(end - spans[0][0]) / 1e3:.1f} ms, idle {g.sum() / 1e3:.1f} ms in {len(gaps)} gaps: "
+                  + ", ".join(f"{(g[(g >= lo) & (g < hi)]).sum() / 1e3:.1f} ms in {int(((g >= lo) & (g < hi)).sum())} "
+                              f"gaps of {lo:g}-{hi:g} us"
+                              for lo, hi in ((0, 5), (5, 20), (20, 100), (100, 1e3), (1e3, 1e9))))
 
 
 def _neo_box(n, traction=None, stretch=None):

@@ -1246,6 +1246,188 @@ pcgx_update_tile_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
   reduce_and_finalize<2>(dv, C, op, partials, C->ticket + 1, nullptr);
 }
 
+// ---- bulk-copy staged form of pcgx_update_tile_kernel (vec 3, general storage) --------
+// A tile's x, r, q (hi and lo), p and preconditioner blocks are eight contiguous runs, so each
+// warp streams whole 32-node tiles through a ring of UPD_STAGES shared-memory stages with 1-D
+// cp.async.bulk copies (lane 0 issues, one mbarrier per stage) and computes on one tile while the
+// next ones are in flight; the plain-load kernel above had only the current tile's loads in
+// flight per warp.  Same arithmetic per dof; x, r and z are stored straight from registers.  The
+// partial last tile (n_nodes % 32 nodes) is filled with plain loads into a drained stage.
+constexpr int UPD_WARPS = 4;
+constexpr int UPD_STAGES = 3;
+
+template <int PC>
+struct UpdGeom {
+  static constexpr int PCW = PC == FEM_PC_BJACOBI ? 9 : PC == FEM_PC_JACOBI ? 3 : 0;
+  static constexpr uint32_t VB = 96 * 4;        // one dof-ordered float array of a tile
+  static constexpr uint32_t PB = 32 * 4 * 8;    // p: 32 nodes x 4 (hi, lo) pairs
+  static constexpr uint32_t CB = 32 * PCW * 4;  // preconditioner blocks
+  static constexpr uint32_t STAGE = 6 * VB + PB + CB;
+  static constexpr uint32_t BAR_BYTES = 128;    // UPD_WARPS * UPD_STAGES barriers, padded
+  static constexpr uint32_t SMEM = BAR_BYTES + UPD_WARPS * UPD_STAGES * STAGE;
+};
+
+template <int PC>
+__global__ void __launch_bounds__(UPD_WARPS * 32)
+pcgx_update_bulk_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restrict__ xl, float* __restrict__ rh,
+                        float* __restrict__ rl, float* __restrict__ z, const float2* __restrict__ pp,
+                        const float* __restrict__ qh, const float* __restrict__ ql, const float* __restrict__ pc,
+                        KCtl* C, double* partials, int op) {
+  using G = UpdGeom<PC>;
+  constexpr int PCW = G::PCW;
+  extern __shared__ __align__(128) unsigned char smem[];
+  if (C->done) return;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem) + wib * UPD_STAGES;
+  unsigned char* ring = smem + G::BAR_BYTES + (size_t)wib * UPD_STAGES * G::STAGE;
+  const int64_t nfull = n_nodes / 32;   // whole tiles, streamed by bulk copies
+  const int64_t nw = (int64_t)gridDim.x * UPD_WARPS;
+  const int64_t warp = (int64_t)blockIdx.x * UPD_WARPS + wib;
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < UPD_STAGES; ++j) mbar_init(bars + j, 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+  const df2 a = df_of(C->alpha);
+  const df2 na{-a.h, -a.l};
+  float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f;
+
+  int64_t pt = warp;  // producer cursor: next whole tile to copy
+  auto produce = [&](int stage) -> bool {
+    if (pt >= nfull) return false;
+    if (lane == 0) {
+      unsigned char* st = ring + (size_t)stage * G::STAGE;
+      uint64_t* bar = bars + stage;
+      const int64_t d0 = pt * 96;
+      async_proxy_fence();
+      mbar_expect_tx(bar, G::STAGE);
+      bulk_load(st, xh + d0, G::VB, bar);
+      bulk_load(st + G::VB, xl + d0, G::VB, bar);
+      bulk_load(st + 2 * G::VB, rh + d0, G::VB, bar);
+      bulk_load(st + 3 * G::VB, rl + d0, G::VB, bar);
+      bulk_load(st + 4 * G::VB, qh + d0, G::VB, bar);
+      bulk_load(st + 5 * G::VB, ql + d0, G::VB, bar);
+      bulk_load(st + 6 * G::VB, pp + pt * 128, G::PB, bar);
+      if constexpr (PCW > 0) bulk_load(st + 6 * G::VB + G::PB, pc + pt * 32 * PCW, G::CB, bar);
+    }
+    pt += nw;
+    return true;
+  };
+
+  // one tile of nn nodes staged at st: x += a p, r -= a q (df), z = M r.h (FP32), dots r.z, r.r
+  auto compute = [&](unsigned char* st, int64_t t, int nn) {
+    float* sxh = reinterpret_cast<float*>(st);
+    float* sxl = sxh + 96;
+    float* srh = sxh + 192;
+    float* srl = sxh + 288;
+    float* sqh = sxh + 384;   // q.h, then z
+    const float* sql = sxh + 480;
+    const float2* spp = reinterpret_cast<const float2*>(st + 6 * G::VB);
+    const float* spc = reinterpret_cast<const float*>(st + 6 * G::VB + G::PB);
+    const int nd = 3 * nn;
+    const int64_t d0 = t * 96;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int o = 32 * j + lane;
+      if (o < nd) {
+        const int nl = o / 3, c = o - 3 * nl;
+        const float2 pv = spp[nl * 4 + c];
+        const df2 x = df_add(df2{sxh[o], sxl[o]}, df_mul(a, df2{pv.x, pv.y}));
+        xh[d0 + o] = x.h;
+        xl[d0 + o] = x.l;
+        const df2 r = df_add(df2{srh[o], srl[o]}, df_mul(na, df2{sqh[o], sql[o]}));
+        rh[d0 + o] = r.h;
+        rl[d0 + o] = r.l;
+        srh[o] = r.h;
+        srl[o] = r.l;
+      }
+    }
+    __syncwarp();
+    if (lane < nn) {
+      const float rv[3] = {srh[3 * lane], srh[3 * lane + 1], srh[3 * lane + 2]};
+      float zv[3];
+      if constexpr (PC == FEM_PC_BJACOBI) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          zv[c] = spc[9 * lane + 3 * c] * rv[0] + spc[9 * lane + 3 * c + 1] * rv[1] + spc[9 * lane + 3 * c + 2] * rv[2];
+      } else if constexpr (PC == FEM_PC_JACOBI) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) zv[c] = spc[3 * lane + c] * rv[c];
+      } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) zv[c] = rv[c];
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        sqh[3 * lane + c] = zv[c];
+        const df2 r{rv[c], srl[3 * lane + c]};
+        df_acc(s0, e0, r, df2{zv[c], 0.f});
+        df_acc(s1, e1, r, r);
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int o = 32 * j + lane;
+      if (o < nd) z[d0 + o] = sqh[o];
+    }
+    async_proxy_fence();   // this lane's shared-memory writes before the stage's next bulk copy
+    __syncwarp();
+  };
+
+  uint32_t parity = 0;  // bit j: phase parity to wait for on stage j
+  int inflight = 0;
+  for (int j = 0; j < UPD_STAGES; ++j) inflight += produce(j) ? 1 : 0;
+  int stage = 0;
+  bool fault = false;
+  for (int64_t t = warp; t < nfull; t += nw) {
+    const bool ok = mbar_wait(bars + stage, (parity >> stage) & 1u);
+    if (!__all_sync(0xffffffffu, ok)) { fault = true; break; }
+    parity ^= 1u << stage;
+    --inflight;
+    compute(ring + (size_t)stage * G::STAGE, t, 32);
+    inflight += produce(stage) ? 1 : 0;
+    stage = stage + 1 == UPD_STAGES ? 0 : stage + 1;
+  }
+  if (fault) {
+    // let the copies already issued land (bounded) before the CTA's shared memory is released
+    for (int j = 0; j < inflight; ++j) {
+      (void)mbar_wait(bars + stage, (parity >> stage) & 1u);
+      parity ^= 1u << stage;
+      stage = stage + 1 == UPD_STAGES ? 0 : stage + 1;
+    }
+    if (lane == 0) {
+      atomicExch(&C->fault, 1);
+      atomicExch(&C->done, 1);
+    }
+  } else if (n_nodes % 32 != 0 && warp == nfull % nw) {
+    // partial last tile: plain loads into stage 0 (every copy of this warp has landed)
+    const int nn = (int)(n_nodes - nfull * 32);
+    const int64_t d0 = nfull * 96;
+    float* s = reinterpret_cast<float*>(ring);
+    for (int o = lane; o < 96; o += 32) {
+      const bool in = o < 3 * nn;
+      s[o] = in ? xh[d0 + o] : 0.f;
+      s[96 + o] = in ? xl[d0 + o] : 0.f;
+      s[192 + o] = in ? rh[d0 + o] : 0.f;
+      s[288 + o] = in ? rl[d0 + o] : 0.f;
+      s[384 + o] = in ? qh[d0 + o] : 0.f;
+      s[480 + o] = in ? ql[d0 + o] : 0.f;
+    }
+    float2* spp = reinterpret_cast<float2*>(ring + 6 * G::VB);
+    for (int o = lane; o < 128; o += 32) spp[o] = o < 4 * nn ? pp[nfull * 128 + o] : make_float2(0.f, 0.f);
+    if constexpr (PCW > 0) {
+      float* spc = reinterpret_cast<float*>(ring + 6 * G::VB + G::PB);
+      for (int o = lane; o < 32 * PCW; o += 32) spc[o] = o < PCW * nn ? pc[nfull * 32 * PCW + o] : 0.f;
+    }
+    __syncwarp();
+    compute(ring, nfull, nn);
+  }
+  double dv[3] = {(double)s0 + (double)e0, (double)s1 + (double)e1, 0.0};
+  reduce_and_finalize<2>(dv, C, op, partials, C->ticket + 1, nullptr);
+}
+
 // vec-3 form of pcgx_direction_kernel, thread per dof: z coalesced, p gathered within the tile.
 __global__ void pcgx_direction3_kernel(int64_t n, const float* __restrict__ z, float2* __restrict__ pp,
                                        const KCtl* C) {
@@ -1586,6 +1768,36 @@ static int poll(KCtl* C, cudaStream_t s, KCtl* host) {
 }
 
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+// The mixed CG's update (vec 3, general storage) by the bulk-copy staged kernel; false when an
+// array is not 16-byte aligned (the caller then launches pcgx_update_tile_kernel).  Grid:
+// resident CTAs, capped by the tiles.
+template <int PC>
+static bool launch_update_bulk(int64_t n_nodes, float* xh, float* xl, float* rh, float* rl, float* z,
+                               const float2* pp, const float* qh, const float* ql, const float* pc, KCtl* C,
+                               double* partials, int op, cudaStream_t s) {
+  using G = UpdGeom<PC>;
+  if (!(aligned16(xh) && aligned16(xl) && aligned16(rh) && aligned16(rl) && aligned16(pp) && aligned16(qh) &&
+        aligned16(ql) && (G::PCW == 0 || aligned16(pc))))
+    return false;
+  auto kern = pcgx_update_bulk_kernel<PC>;
+  constexpr int smem = (int)G::SMEM;
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, UPD_WARPS * 32, smem) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+  }
+  int64_t g = (int64_t)sm_count() * per_sm;
+  const int64_t need = ((n_nodes + 31) / 32 + UPD_WARPS - 1) / UPD_WARPS;
+  if (g > need) g = need;
+  if (g > MAX_PARTIAL_BLOCKS) g = MAX_PARTIAL_BLOCKS;
+  if (g < 1) g = 1;
+  kern<<<(unsigned)g, UPD_WARPS * 32, smem, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C, partials, op);
+  return true;
+}
 
 // The mixed CG's SpMV: bulk-copy staged kernel for vec 3 when the streamed arrays are 16-byte
 // aligned, the register-streaming kernel otherwise.  Grid: resident CTAs, capped by the slices.
@@ -1953,8 +2165,10 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
         rc = launch_dfdf<VEC, SYM>(pat, n_nodes, vhi, vlo, pp, qh, ql, C, FIN_PCG_ALPHA, w.partials, s, qT);
         if (rc) return rc;
         if constexpr (VEC == 3) {
-          pcgx_update_tile_kernel<PC, SYM><<<gt, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
-                                                                   w.partials, FIN_PCGR_UPDATE, qT);
+          if (SYM || !launch_update_bulk<PC>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C, w.partials,
+                                             FIN_PCGR_UPDATE, s))
+            pcgx_update_tile_kernel<PC, SYM><<<gt, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
+                                                                     w.partials, FIN_PCGR_UPDATE, qT);
           pcgx_direction3_kernel<<<gv, VTHREADS, 0, s>>>(n, z, pp, C);
         } else {
           pcgx_update_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
