@@ -251,7 +251,47 @@ cell_kernel(const AsmParams P) {
     const int64_t row = (int64_t)na * VEC + i;
     const bool row_bc = active && P.bc && P.bc[row];
 
-    if (want_mat && active && !(row_bc && P.bc_mode != FEM_BC_NONE)) {
+    if constexpr (TAN == TAN_ISO && VEC == 3) {
+      if (want_mat && active && !(row_bc && P.bc_mode != FEM_BC_NONE)) {
+        // K[(a,i),(b,k)] = sum_q lam g_a,i g_b,k + mu g_a,k g_b,i + mu (g_a . g_b) delta_ik, with
+        // this thread's three columns rotated so that m = 0 is k = i (k = (i + m) mod 3): the
+        // diagonal term then lands on a fixed accumulator and, with g_b,i = g_b,k there, the
+        // three m = 0 terms fold into one coefficient lam g_a,i + 2 mu g_a,i.  Seven FMAs per
+        // (qp, b); the three threads of node a no longer repeat a select-and-add per column.
+        const int i1 = i == 2 ? 0 : i + 1, i2 = i == 0 ? 2 : i - 1;
+        T acc[NN][3];
+        for (int b = 0; b < NN; ++b) acc[b][0] = acc[b][1] = acc[b][2] = T(0);
+        for (int q = 0; q < NQ; ++q) {
+          const T* G = sG + (c * NQ + q) * NN * 3;
+          const T* tq = sTan + (c * NQ + q) * NTAN;
+          const T lam = tq[0], mu = tq[1];
+          const T ga0 = G[a * 3 + i], ga1 = G[a * 3 + i1], ga2 = G[a * 3 + i2];
+          const T m0 = mu * ga0, m1 = mu * ga1, m2 = mu * ga2;
+          const T c0 = lam * ga0 + T(2) * m0;
+          const T l0 = lam * ga0;
+#pragma unroll
+          for (int b = 0; b < NN; ++b) {
+            const T gb0 = G[b * 3 + i], gb1 = G[b * 3 + i1], gb2 = G[b * 3 + i2];
+            acc[b][0] = fma(c0, gb0, fma(m1, gb1, fma(m2, gb2, acc[b][0])));
+            acc[b][1] = fma(l0, gb1, fma(m1, gb0, acc[b][1]));
+            acc[b][2] = fma(l0, gb2, fma(m2, gb0, acc[b][2]));
+          }
+        }
+        T* vals = reinterpret_cast<T*>(P.vals);
+        const int64_t rs = P.indptr[row];
+        const uint8_t* sl = P.slots + (e * NN + a) * NN;
+        const int kk[3] = {i, i1, i2};
+        for (int b = 0; b < NN; ++b) {
+          const int nb = sConn[c * NN + b];
+          T* dst = vals + rs + (int64_t)3 * sl[b];
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            if (P.bc_mode == FEM_BC_SYMMETRIC && P.bc[(int64_t)nb * 3 + kk[m]]) continue;
+            atomicAdd(dst + kk[m], acc[b][m]);
+          }
+        }
+      }
+    } else if (want_mat && active && !(row_bc && P.bc_mode != FEM_BC_NONE)) {
       T acc[NN][VEC];
       for (int b = 0; b < NN; ++b)
         for (int k = 0; k < VEC; ++k) acc[b][k] = T(0);

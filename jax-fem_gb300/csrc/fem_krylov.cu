@@ -34,6 +34,7 @@ struct KCtl {
   long long iter, maxiter;
   int done, status, exit_early, fault;   // fault: a bounded device wait ran out
   unsigned int ticket[4];
+  float alpha_h, alpha_l, beta_h, beta_l;   // alpha, beta as float pairs for the double-float kernels
 };
 
 static bool is_sliced(int p) { return p == FEM_SLICED_F32 || p == FEM_SLICED_F64 || p == FEM_SLICED_DF48 || p == FEM_SYM_DF48; }
@@ -151,6 +152,12 @@ __device__ void finalize(KCtl* C, int op, const double (&d)[3], double* dot_out)
     default:
       break;
   }
+  // split once here: every thread of the double-float kernels would otherwise convert from FP64,
+  // and a warp-wide FP64 instruction takes tens of cycles of GB300's FP64 pipe
+  C->alpha_h = __double2float_rn(C->alpha);
+  C->alpha_l = __double2float_rn(C->alpha - (double)C->alpha_h);
+  C->beta_h = __double2float_rn(C->beta);
+  C->beta_l = __double2float_rn(C->beta - (double)C->beta_h);
 }
 
 // Per-CTA partial sums of up to 3 dots, last CTA finalizes.
@@ -259,6 +266,71 @@ __device__ __forceinline__ void df_acc(float& sh, float& sl, df2 a, df2 b) {
   two_sum(sh, p, t, te);
   sl += te + e;
   sh = t;
+}
+
+// Double-float form of reduce_and_finalize for the double-float kernels: per-thread pairs are
+// summed in double-float on the FP32 pipes (shuffles within a warp, then one warp over the warps'
+// sums), each CTA stores its pairs as floats in its partials slot, and the last CTA sums the slots
+// in block order, again in double-float; one thread converts the totals to FP64 for finalize.
+// GB300's FP64 pipe takes tens of cycles per warp-wide instruction, so an FP64 epilogue run by
+// every warp of an SM at once costs microseconds per launch.
+__device__ __forceinline__ df2 df_shfl_down(df2 v, int off) {
+  return df2{__shfl_down_sync(0xffffffffu, v.h, off), __shfl_down_sync(0xffffffffu, v.l, off)};
+}
+template <int ND>
+__device__ __forceinline__ void block_sum_df(df2 (&v)[ND], df2* sh) {  // total in thread 0
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < ND; ++k)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v[k] = df_add(v[k], df_shfl_down(v[k], off));
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < ND; ++k) sh[k * 32 + wid] = v[k];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+      df2 t = lane < nw ? sh[k * 32 + lane] : df2{0.f, 0.f};
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) t = df_add(t, df_shfl_down(t, off));
+      v[k] = t;
+    }
+  }
+  __syncthreads();
+}
+template <int ND>
+__device__ __forceinline__ void reduce_and_finalize_df(df2 (&v)[ND], KCtl* C, int op, double* partials,
+                                                       unsigned* ticket, double* dot_out) {
+  __shared__ df2 sh[3 * 32];
+  block_sum_df<ND>(v, sh);
+  float* pf = reinterpret_cast<float*>(partials);   // a block's 3 double slots hold 3 float pairs
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+      pf[(size_t)blockIdx.x * 6 + 2 * k] = v[k].h;
+      pf[(size_t)blockIdx.x * 6 + 2 * k + 1] = v[k].l;
+    }
+  }
+  if (last_block_ticket(ticket)) {
+    df2 acc[ND];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) acc[k] = df2{0.f, 0.f};
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+      const volatile float* p = pf + (size_t)b * 6;
+#pragma unroll
+      for (int k = 0; k < ND; ++k) acc[k] = df_add(acc[k], df2{p[2 * k], p[2 * k + 1]});
+    }
+    block_sum_df<ND>(acc, sh);
+    if (threadIdx.x == 0) {
+      double tot[3] = {0, 0, 0};
+#pragma unroll
+      for (int k = 0; k < ND; ++k) tot[k] = (double)acc[k].h + (double)acc[k].l;
+      finalize(C, op, tot, dot_out);
+    }
+  }
 }
 
 template <int FMT>
@@ -530,8 +602,8 @@ spmv_sliced_dfdf_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* __rest
       }
     }
   }
-  double dv[3] = {(double)ds + (double)de, 0.0, 0.0};
-  reduce_and_finalize<1>(dv, C, op, partials, C->ticket, &C->d0);
+  df2 dv[1] = {df2{ds, de}};
+  reduce_and_finalize_df<1>(dv, C, op, partials, C->ticket, &C->d0);
 }
 
 // ---- bulk-copy (TMA engine) staging for the sliced DF48 SpMV -------------------------
@@ -771,9 +843,9 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
       atomicExch(&C->done, 1);
     }
   }
-  double dv[3] = {(double)ds + (double)de, 0.0, 0.0};
-  if constexpr (SYM) dv[0] = 2.0 * dv[0] - ((double)dd_h + (double)dd_l);
-  reduce_and_finalize<1>(dv, C, op, partials, C->ticket, &C->d0);
+  df2 dv[1] = {df2{ds, de}};
+  if constexpr (SYM) dv[0] = df_add(df2{2.f * ds, 2.f * de}, df2{-dd_h, -dd_l});
+  reduce_and_finalize_df<1>(dv, C, op, partials, C->ticket, &C->d0);
 }
 
 // y (df) += qT (FP64, component-major: component c of node i at c * n_nodes + i), qT = 0: the
@@ -1109,8 +1181,8 @@ __global__ void pcgx_start_kernel(int64_t n_nodes, const float* rh, const float*
       df_acc(s1, e1, r, r);
     }
   }
-  double dv[3] = {(double)s0 + (double)e0, (double)s1 + (double)e1, 0.0};
-  reduce_and_finalize<2>(dv, C, FIN_PCGR_START, partials, C->ticket + 1, nullptr);
+  df2 dv[2] = {df2{s0, e0}, df2{s1, e1}};
+  reduce_and_finalize_df<2>(dv, C, FIN_PCGR_START, partials, C->ticket + 1, nullptr);
 }
 
 // x += alpha p ; r -= alpha q ; z = M r.h ; dots (r.z, r.r)
@@ -1120,7 +1192,7 @@ __global__ void pcgx_update_kernel(int64_t n_nodes, float* xh, float* xl, float*
                                    KCtl* C, double* partials, int op) {
   constexpr int PAD = DfNode<VEC>::PAD;
   if (C->done) return;
-  const df2 a = df_of(C->alpha);
+  const df2 a{C->alpha_h, C->alpha_l};
   const df2 na{-a.h, -a.l};
   float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f;
   GRID_STRIDE_NODES(i, n_nodes) {
@@ -1146,8 +1218,8 @@ __global__ void pcgx_update_kernel(int64_t n_nodes, float* xh, float* xl, float*
       df_acc(s1, e1, rr[c], rr[c]);
     }
   }
-  double dv[3] = {(double)s0 + (double)e0, (double)s1 + (double)e1, 0.0};
-  reduce_and_finalize<2>(dv, C, op, partials, C->ticket + 1, nullptr);
+  df2 dv[2] = {df2{s0, e0}, df2{s1, e1}};
+  reduce_and_finalize_df<2>(dv, C, op, partials, C->ticket + 1, nullptr);
 }
 
 // vec-3 form of pcgx_update_kernel with every global access coalesced: a warp takes a tile of
@@ -1168,7 +1240,7 @@ pcgx_update_tile_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
   __shared__ float s_r[VTILE_WARPS][96], s_rl[VTILE_WARPS][96], s_z[VTILE_WARPS][96];
   __shared__ float s_pc[VTILE_WARPS][PCW > 0 ? 32 * PCW : 1];
   if (C->done) return;
-  const df2 a = df_of(C->alpha);
+  const df2 a{C->alpha_h, C->alpha_l};
   const df2 na{-a.h, -a.l};
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   float* sr = s_r[w];
@@ -1242,8 +1314,8 @@ pcgx_update_tile_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
     }
     __syncwarp();
   }
-  double dv[3] = {(double)s0 + (double)e0, (double)s1 + (double)e1, 0.0};
-  reduce_and_finalize<2>(dv, C, op, partials, C->ticket + 1, nullptr);
+  df2 dv[2] = {df2{s0, e0}, df2{s1, e1}};
+  reduce_and_finalize_df<2>(dv, C, op, partials, C->ticket + 1, nullptr);
 }
 
 // ---- bulk-copy staged form of pcgx_update_tile_kernel (vec 3, general storage) --------
@@ -1289,7 +1361,7 @@ pcgx_update_bulk_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
     mbar_init_fence();
   }
   __syncwarp();
-  const df2 a = df_of(C->alpha);
+  const df2 a{C->alpha_h, C->alpha_l};
   const df2 na{-a.h, -a.l};
   float s0 = 0.f, e0 = 0.f, s1 = 0.f, e1 = 0.f;
 
@@ -1424,15 +1496,15 @@ pcgx_update_bulk_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
     __syncwarp();
     compute(ring, nfull, nn);
   }
-  double dv[3] = {(double)s0 + (double)e0, (double)s1 + (double)e1, 0.0};
-  reduce_and_finalize<2>(dv, C, op, partials, C->ticket + 1, nullptr);
+  df2 dv[2] = {df2{s0, e0}, df2{s1, e1}};
+  reduce_and_finalize_df<2>(dv, C, op, partials, C->ticket + 1, nullptr);
 }
 
 // vec-3 form of pcgx_direction_kernel, thread per dof: z coalesced, p gathered within the tile.
 __global__ void pcgx_direction3_kernel(int64_t n, const float* __restrict__ z, float2* __restrict__ pp,
                                        const KCtl* C) {
   if (C->done) return;
-  const df2 b = df_of(C->beta);
+  const df2 b{C->beta_h, C->beta_l};
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = k / 3;
     const int64_t o = i * 4 + (k - 3 * i);
@@ -1447,7 +1519,7 @@ template <int VEC>
 __global__ void pcgx_direction_kernel(int64_t n_nodes, const float* z, float2* pp, const KCtl* C) {
   constexpr int PAD = DfNode<VEC>::PAD;
   if (C->done) return;
-  const df2 b = df_of(C->beta);
+  const df2 b{C->beta_h, C->beta_l};
   GRID_STRIDE_NODES(i, n_nodes) {
 #pragma unroll
     for (int c = 0; c < VEC; ++c) {
@@ -1586,6 +1658,7 @@ __global__ void init_ctl_kernel(KCtl* C, double thresh2_rel, double atol2, long 
     C->done = 0; C->status = 0; C->exit_early = 0; C->fault = 0;
     C->thresh2 = thresh2_rel; C->d1 = atol2; C->maxiter = maxiter; C->iter = 0;
     C->ticket[0] = C->ticket[1] = C->ticket[2] = C->ticket[3] = 0;
+    C->alpha_h = C->alpha_l = C->beta_h = C->beta_l = 0.f;
   }
 }
 

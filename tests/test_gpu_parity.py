@@ -252,6 +252,30 @@ def test_mixed_precision_matches_fp64(cuda, mode):
     assert np.abs(gmx - g64).max() <= 1e-8 * np.abs(g64).max()
 
 
+@pytest.mark.parametrize("n", [(1, 1, 1), (3, 1, 1), (4, 2, 1), (3, 3, 3), (5, 3, 2)])
+def test_small_and_ragged_meshes(cuda, n):
+    """Meshes of 8, 16, 30, 64 and 72 nodes: below one 32-node tile (the update kernels' partial
+    tile only), exactly two tiles (no partial tile) and a ragged last tile.  FP64 and mixed
+    solutions and the mixed gradient against the oracle's direct solve and implicit_vjp (1e-10 /
+    1e-9 / 1e-8 relative)."""
+    import cases
+    from oracle import solve as osolve
+    prob, oprob, theta_np = cases.simp_box(*n)
+    oprob.internal_vars = cases.oracle_set_params(oprob, torch.tensor(theta_np))
+    osol = osolve.newton_solve(oprob, {"spsolve_solver": {}})
+    fo = prob._engine.f_ext.cpu().numpy().copy()
+    fo[oprob.bc_rows()[0]] = 0.0
+    g_or, _ = osolve.implicit_vjp(oprob, osol, theta_np, cases.oracle_set_params, fo)
+    scale = np.abs(osol).max()
+    for mode, tol in (("fp64", 1e-10), ("mixed", 1e-9)):
+        lin = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}}
+        if mode == "mixed":
+            lin["precision"] = "mixed"
+        sol, _, g = _simp_grad(prob, theta_np, cuda, dict(lin, rel_tol=1e-12, tol=0.0), lin)
+        assert np.abs(sol.cpu().numpy() - osol).max() <= tol * scale, mode
+        assert np.abs(g - g_or).max() <= 1e-8 * np.abs(g_or).max(), mode
+
+
 def test_tet10_pattern_and_values(cuda):
     """TET10 (Kuhn split) pattern bit-exact and FP64 tangent within 1e-12 of the oracle."""
     import jax_fem_gb300 as jf
