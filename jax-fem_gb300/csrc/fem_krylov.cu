@@ -1530,14 +1530,16 @@ __global__ void pcgx_direction_kernel(int64_t n_nodes, const float* z, float2* p
   }
 }
 
-// df <-> FP64 for the reliable updates: x64 = x (df) ; (r.h, r.l) = split(r64)
-__global__ void df_to_f64_kernel(int64_t n, const float* h, const float* l, double* out) {
+// df <-> FP64 for the reliable updates: x64 = x (df) / scale ; (r.h, r.l) = split(r64 * scale).
+// scale is a power of two (exact both ways): it keeps the double-float vectors of a solve near
+// unit size, away from the ends of FP32's exponent range.
+__global__ void df_to_f64_kernel(int64_t n, const float* h, const float* l, double* out, double inv_scale) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    out[k] = (double)h[k] + (double)l[k];
+    out[k] = ((double)h[k] + (double)l[k]) * inv_scale;
 }
-__global__ void f64_to_df_kernel(int64_t n, const double* v, float* h, float* l) {
+__global__ void f64_to_df_kernel(int64_t n, const double* v, float* h, float* l, double scale) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-    const df2 d = df_of(v[k]);
+    const df2 d = df_of(v[k] * scale);
     h[k] = d.h;
     l[k] = d.l;
   }
@@ -2181,17 +2183,15 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
   if (gt < 1) gt = 1;
   init_ctl_kernel<<<1, 32, 0, s>>>(C, rtol * rtol, atol * atol, (long long)maxiter);
   dot_kernel<double><<<gv, VTHREADS, 0, s>>>(n, b, b, C, w.partials, nullptr, FIN_REF_BB);
-  f64_to_df_kernel<<<gv, VTHREADS, 0, s>>>(n, x, xh, xl);
-  note_launches(3);
+  note_launches(2);
   int rc = check_launch("pcg_dfx init");
   if (rc) return rc;
-  // FP64 true residual at the FP64 iterate held in x; r (df) := split(r64)
+  // FP64 true residual at the FP64 iterate held in x, and ||r||^2
   auto true_residual = [&]() -> int {
     const int r2 = ref_apply<VEC>(pat, n_nodes, op, x, ax, s);
     if (r2) return r2;
     refine_residual64_kernel<<<gv, VTHREADS, 0, s>>>(n, b, x, ax, bc, r64, C, w.partials);
-    f64_to_df_kernel<<<gv, VTHREADS, 0, s>>>(n, r64, rh, rl);
-    note_launches(2);
+    note_launches(1);
     return check_launch("refine_residual (df)");
   };
   rc = true_residual();
@@ -2199,11 +2199,26 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
   KCtl h;
   rc = poll(C, s, &h);
   if (rc) return rc;
+  // The double-float vectors carry x and r times a power of two that brings the initial residual's
+  // RMS near 1, so that r, z, p, q and their dot products stay inside FP32's range (products near
+  // 1e-38 would lose precision in subnormals, above 3e38 overflow) however the problem is scaled.
+  // Every step of the iteration commutes exactly with a power-of-two scale.
+  double scale = 1.0;
+  if (h.rr_true > 0.0 && std::isfinite(h.rr_true)) {
+    const int e = std::ilogb(std::sqrt(h.rr_true / (double)n));
+    scale = std::ldexp(1.0, -std::max(-900, std::min(900, e)));
+  }
+  const double inv_scale = 1.0 / scale;
+  f64_to_df_kernel<<<gv, VTHREADS, 0, s>>>(n, x, xh, xl, scale);
+  f64_to_df_kernel<<<gv, VTHREADS, 0, s>>>(n, r64, rh, rl, scale);
+  note_launches(2);
   int64_t n_updates = 0;
   int final_status = FEM_SOLVE_CONVERGED;
   const double delta2 = delta * delta;
+  const double check2 = h.check2 * scale * scale;   // the pause test runs on the scaled recursive residual
   if (!(h.rr_true <= h.thresh2)) {
     FEM_CUDA(cudaMemcpyAsync(&C->delta2, &delta2, sizeof(double), cudaMemcpyHostToDevice, s));
+    FEM_CUDA(cudaMemcpyAsync(&C->check2, &check2, sizeof(double), cudaMemcpyHostToDevice, s));
     pcgx_start_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, rh, rl, z, pp, pc, 1, C, w.partials);
     note_launches(1);
     int64_t launched = 0;
@@ -2213,10 +2228,12 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
       if (h.done) {
         if (h.status == SOLVE_UPDATE || h.status == FEM_SOLVE_MAXITER) {
           const bool at_max = h.status == FEM_SOLVE_MAXITER;
-          df_to_f64_kernel<<<gv, VTHREADS, 0, s>>>(n, xh, xl, x);
+          df_to_f64_kernel<<<gv, VTHREADS, 0, s>>>(n, xh, xl, x, inv_scale);
           note_launches(1);
           rc = true_residual();
           if (rc) return rc;
+          f64_to_df_kernel<<<gv, VTHREADS, 0, s>>>(n, r64, rh, rl, scale);
+          note_launches(1);
           rc = poll(C, s, &h);
           if (rc) return rc;
           ++n_updates;
@@ -2229,7 +2246,7 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
           continue;
         }
         final_status = h.status;  // NaN or breakdown
-        df_to_f64_kernel<<<gv, VTHREADS, 0, s>>>(n, xh, xl, x);
+        df_to_f64_kernel<<<gv, VTHREADS, 0, s>>>(n, xh, xl, x, inv_scale);
         note_launches(1);
         break;
       }

@@ -140,8 +140,9 @@ def plasticity(g):
     return prob, bc, disps
 
 
-def simp_box(nx, ny, nz, L=(2.0, 1.0, 0.5), seed=0, theta=None):
-    """SIMP cantilever: clamped x=0, traction on x=Lx face, theta = 0.5 + U(-0.05, 0.05)."""
+def simp_box(nx, ny, nz, L=(2.0, 1.0, 0.5), seed=0, theta=None, load=1.0):
+    """SIMP cantilever: clamped x=0, traction on x=Lx face (surface map (0, 0, load)),
+    theta = 0.5 + U(-0.05, 0.05)."""
     Lx, Ly, Lz = L
     m = jf.box_mesh(nx, ny, nz, Lx, Ly, Lz)
     points, cells = m.points, m.cells_dict["hexahedron"]
@@ -155,7 +156,7 @@ def simp_box(nx, ny, nz, L=(2.0, 1.0, 0.5), seed=0, theta=None):
             return jf.SIMPElastic(1.0, 1e-3, 0.3, 3.0)
 
         def get_surface_maps(self):
-            return [lambda u, x: np.array([0.0, 0.0, 1.0])]
+            return [lambda u, x: np.array([0.0, 0.0, load])]
 
         def set_params(self, params):
             self.internal_vars = [params[:, None, :].expand(-1, 8, -1)]
@@ -163,7 +164,7 @@ def simp_box(nx, ny, nz, L=(2.0, 1.0, 0.5), seed=0, theta=None):
     prob = P(jf.Mesh(points, cells), vec=3, dim=3, dirichlet_bc_info=bc, location_fns=[right])
     oprob = ofem.OracleProblem(points, cells, 3, dirichlet_bc_info=bc, location_fns=[right],
                                tensor_map=omat.simp_elastic(1.0, 1e-3, 0.3, 3.0),
-                               surface_maps=[lambda u, x: torch.tensor([0.0, 0.0, 1.0])])
+                               surface_maps=[lambda u, x: torch.tensor([0.0, 0.0, load])])
     if theta is None:
         rng = np.random.default_rng(seed)
         theta = 0.5 + rng.uniform(-0.05, 0.05, size=(len(cells), 1))
