@@ -1045,11 +1045,11 @@ __global__ void pcg_update_kernel(int64_t n_nodes, T* x, T* r, T* z, const T* p,
 // Reliable-update PCG: FP64 true residual r64 = b - A x (A x in ax; Dirichlet rows b - x),
 // its FP32 copy r32, and ||r64||^2.
 __global__ void refine_residual_kernel(int64_t n, const double* b, const double* x, const double* ax,
-                                       const uint8_t* bc, float* r32, KCtl* C, double* partials) {
+                                       const uint8_t* bc, float* r32, KCtl* C, double* partials, double scale) {
   double dv[3] = {0, 0, 0};
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
     const double r = (bc && bc[k]) ? (b[k] - x[k]) : (b[k] - ax[k]);
-    r32[k] = (float)r;
+    r32[k] = (float)(r * scale);   // scale: a power of two keeping the FP32 iteration near unit size
     dv[0] += r * r;
   }
   reduce_and_finalize<1>(dv, C, FIN_REF_TRUE, partials, C->ticket + 1, nullptr);
@@ -1078,9 +1078,9 @@ __global__ void pcgr_start_kernel(int64_t n_nodes, const float* r, float* z, flo
   reduce_and_finalize<2>(dv, C, FIN_PCGR_START, partials, C->ticket + 1, nullptr);
 }
 
-__global__ void accumulate_kernel(double* x64, const float* x32, int64_t n) {
+__global__ void accumulate_kernel(double* x64, const float* x32, int64_t n, double inv_scale) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    x64[k] += (double)x32[k];
+    x64[k] += (double)x32[k] * inv_scale;
 }
 
 // ---- double-float (DF48) PCG: FP64 vectors, DF48 SpMV, FP32 preconditioner --------
@@ -2052,16 +2052,28 @@ static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const flo
   note_launches(2);
   int rc = check_launch("pcg_refined init");
   if (rc) return rc;
+  KCtl h;
+  rc = poll(C, s, &h);
+  if (rc) return rc;
+  // r and the correction x32 are carried times a power of two that brings b's RMS near 1 (fixed
+  // for the solve), so that the FP32 iteration stays inside FP32's exponent range however the
+  // problem is scaled; the pause threshold on the recursive residual is rescaled to match.
+  double scale = 1.0;
+  if (h.bb > 0.0 && std::isfinite(h.bb)) {
+    const int e = std::ilogb(std::sqrt(h.bb / (double)n));
+    scale = std::ldexp(1.0, -std::max(-900, std::min(900, e)));
+  }
+  const double inv_scale = 1.0 / scale;
+  const double check2 = h.check2 * scale * scale;
   auto true_residual = [&]() -> int {
     const int r2 = ref_apply<VEC>(pat, n_nodes, op, x, ax, s);
     if (r2) return r2;
-    refine_residual_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(n, b, x, ax, bc, r, C, w.partials);
+    refine_residual_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(n, b, x, ax, bc, r, C, w.partials, scale);
     note_launches(1);
     return check_launch("refine_residual");
   };
   rc = true_residual();
   if (rc) return rc;
-  KCtl h;
   rc = poll(C, s, &h);
   if (rc) return rc;
   int64_t n_updates = 0;
@@ -2070,6 +2082,7 @@ static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const flo
   if (!(h.rr_true <= h.thresh2)) {
     // first start: z = M r, p = z
     FEM_CUDA(cudaMemcpyAsync(&C->delta2, &delta2, sizeof(double), cudaMemcpyHostToDevice, s));
+    FEM_CUDA(cudaMemcpyAsync(&C->check2, &check2, sizeof(double), cudaMemcpyHostToDevice, s));
     pcgr_start_kernel<VEC, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, z, p, x32, pc, 1, C, w.partials);
     note_launches(1);
     int64_t launched = 0;
@@ -2079,7 +2092,7 @@ static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const flo
       if (h.done) {
         if (h.status == SOLVE_UPDATE) {
           // residual replacement: x += x32 in FP64, r = b - A x in FP64
-          accumulate_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(x, x32, n);
+          accumulate_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(x, x32, n, inv_scale);
           note_launches(1);
           rc = true_residual();
           if (rc) return rc;
@@ -2096,7 +2109,7 @@ static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const flo
           continue;
         }
         if (h.status == FEM_SOLVE_MAXITER) {
-          accumulate_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(x, x32, n);
+          accumulate_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(x, x32, n, inv_scale);
           note_launches(1);
           rc = true_residual();
           if (rc) return rc;

@@ -276,16 +276,18 @@ def test_small_and_ragged_meshes(cuda, n):
         assert np.abs(g - g_or).max() <= 1e-8 * np.abs(g_or).max(), mode
 
 
+@pytest.mark.parametrize("mode", ["mixed", "mixed32"])
 @pytest.mark.parametrize("load", [1e-30, 1e25])
-def test_mixed_precision_extreme_scaling(cuda, load):
-    """Loads of 1e-30 and 1e25: the double-float CG's residual products would fall below FP32's
-    normal range (or above its maximum) without the solver's power-of-two vector scaling.  Mixed
-    solution and gradient against FP64 (1e-9 / 1e-8 relative); Newton's absolute tolerance off."""
+def test_mixed_precision_extreme_scaling(cuda, load, mode):
+    """Loads of 1e-30 and 1e25: the FP32-based CG's residual products would fall below FP32's
+    normal range (or above its maximum) without the solvers' power-of-two vector scaling.  Mixed
+    (double-float) and mixed32 (FP32) solution and gradient against FP64 (1e-9 / 1e-8 relative);
+    Newton's absolute tolerance off."""
     import cases
     prob, _, theta_np = cases.simp_box(6, 3, 2, load=load)
     lin = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}}
     s64, _, g64 = _simp_grad(prob, theta_np, cuda, dict(lin, rel_tol=1e-12, tol=0.0), lin)
-    lmx = dict(lin, precision="mixed")
+    lmx = dict(lin, precision=mode)
     smx, _, gmx = _simp_grad(prob, theta_np, cuda, dict(lmx, rel_tol=1e-12, tol=0.0), lmx)
     assert np.isfinite(smx.cpu().numpy()).all() and np.isfinite(gmx).all()
     assert (smx - s64).abs().max().item() <= 1e-9 * s64.abs().max().item()
