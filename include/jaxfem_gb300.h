@@ -320,6 +320,12 @@ int fem_axpy_f32_f64(double alpha, const float* x, double* y, int64_t n, void* s
 /* Deterministic FP64 dot product written to *out (device); ws >= fem_krylov_workspace bytes. */
 int fem_dot(int32_t precision, const void* x, const void* y, int64_t n, double* out,
             void* ws, size_t ws_bytes, void* stream);
+/* Failure-detection self-test (no reference counterpart; the reference's solvers do not wait on
+ * the device): one warp waits, through the bounded mbarrier wait of the bulk-copy kernels, on a
+ * phase that never completes; the wait gives up after its limit (~2 s) and the call returns
+ * FEM_ERR_DEVICE exactly as a solver whose copy never landed would.  The context stays usable.
+ * ws >= fem_krylov_workspace(0, FEM_F64) bytes. */
+int fem_selftest_bounded_wait(void* ws, size_t ws_bytes, void* stream);
 
 /* ---- topology-optimisation update (jax_fem/mma.py) ------------------------------------ */
 /* Workspace bytes of fem_mma_update for n design variables and m constraints (1 <= m <= 4). */

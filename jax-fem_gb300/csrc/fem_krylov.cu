@@ -651,6 +651,26 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
+// Failure-detection self-test of the bounded wait above: one warp waits on a phase that can never
+// complete (an mbarrier expecting two arrivals receives one; no copy, no transaction bytes), gives
+// up after the same limit as the bulk-copy kernels and reports the way they do, through the
+// control block's fault and done words.
+__global__ void bounded_wait_selftest_kernel(KCtl* C) {
+  __shared__ __align__(8) uint64_t bar;
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) {
+    mbar_init(&bar, 2);
+    mbar_init_fence();
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&bar)) : "memory");
+  }
+  __syncwarp();
+  const bool ok = mbar_wait(&bar, 0);
+  if (!__all_sync(0xffffffffu, ok) && lane == 0) {
+    atomicExch(&C->fault, 1);
+    atomicExch(&C->done, 1);
+  }
+}
+
 template <int VEC>
 struct BulkGeom {
   static constexpr uint32_t VB = VEC * VEC * 32 * 4;  // value bytes per slot
@@ -2551,6 +2571,20 @@ extern "C" int fem_axpy_f32_f64(double alpha, const float* x, double* y, int64_t
   if (n == 0) return FEM_OK;
   axpy_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(alpha, x, y, n);
   return check_launch("axpy");
+}
+
+extern "C" int fem_selftest_bounded_wait(void* ws, size_t ws_bytes, void* stream) {
+  FEM_REQUIRE(ws, "NULL argument");
+  FEM_REQUIRE(ws_bytes >= al(sizeof(KCtl)) + al(sizeof(double) * 3 * MAX_PARTIAL_BLOCKS), "workspace too small");
+  cudaStream_t s = as_stream(stream);
+  KWs w = carve(ws, 0, FEM_F64);
+  init_ctl_kernel<<<1, 32, 0, s>>>(w.ctl, 0.0, 0.0, 0);
+  bounded_wait_selftest_kernel<<<1, 32, 0, s>>>(w.ctl);
+  note_launches(2);
+  const int rc = check_launch("bounded-wait self-test");
+  if (rc) return rc;
+  KCtl h;
+  return poll(w.ctl, s, &h);   // FEM_ERR_DEVICE when the wait ran out, as designed
 }
 
 extern "C" int fem_dot(int32_t precision, const void* x, const void* y, int64_t n, double* out, void* ws,

@@ -374,6 +374,32 @@ def test_nan_input_is_reported(cuda):
         jf.solver(prob, {"petsc_solver": {"ksp_type": "cg", "pc_type": "jacobi", "rtol": 1e-10}})
 
 
+def test_bounded_wait_reports_and_context_survives(cuda):
+    """The bulk-copy kernels' bounded mbarrier wait, made to run out on a phase that nothing
+    completes (fem_selftest_bounded_wait): the call returns FEM_ERR_DEVICE with the fault message
+    after ~2 s instead of hanging, and the context still runs a mixed solve to the oracle's answer."""
+    import ctypes
+    import time
+    import cases
+    import jax_fem_gb300 as jf
+    from oracle import solve as osolve
+    L = jf._lib
+    nb = ctypes.c_size_t()
+    L.call("fem_krylov_workspace", 0, L.FEM_F64, ctypes.byref(nb))
+    ws = torch.empty(nb.value, dtype=torch.uint8, device=cuda)
+    t0 = time.perf_counter()
+    rc = L.load().fem_selftest_bounded_wait(L.ptr(ws), nb.value, L.stream_handle())
+    waited = time.perf_counter() - t0
+    assert rc == L.FEM_ERR_DEVICE and "bounded device wait" in L.last_error()
+    assert 0.2 < waited < 30.0
+    prob, oprob, theta_np = cases.simp_box(4, 2, 2)
+    lin = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}, "precision": "mixed"}
+    sol, _, _ = _simp_grad(prob, theta_np, cuda, dict(lin, rel_tol=1e-12, tol=0.0), lin)
+    oprob.internal_vars = cases.oracle_set_params(oprob, torch.tensor(theta_np))
+    osol = osolve.newton_solve(oprob, {"spsolve_solver": {}})
+    assert np.abs(sol.cpu().numpy() - osol).max() <= 1e-9 * np.abs(osol).max()
+
+
 def test_maxiter_status(cuda):
     import cases
     import jax_fem_gb300 as jf
