@@ -320,6 +320,12 @@ int fem_axpy_f32_f64(double alpha, const float* x, double* y, int64_t n, void* s
 /* Deterministic FP64 dot product written to *out (device); ws >= fem_krylov_workspace bytes. */
 int fem_dot(int32_t precision, const void* x, const void* y, int64_t n, double* out,
             void* ws, size_t ws_bytes, void* stream);
+/* Measurement hook (no reference counterpart): between start and stop, the mixed CG
+ * (fem_pcg_refined with FEM_SLICED_DF48 / FEM_SYM_DF48) brackets the first SpMV of every
+ * 16-iteration chunk with CUDA events on its stream; stop returns the summed SpMV time and the
+ * number of timed launches.  Process-wide state: not for concurrent solves. */
+int fem_spmv_timing_start(void);
+int fem_spmv_timing_stop(double* seconds, int64_t* samples);
 /* Failure-detection self-test (no reference counterpart; the reference's solvers do not wait on
  * the device): one warp waits, through the bounded mbarrier wait of the bulk-copy kernels, on a
  * phase that never completes; the wait gives up after its limit (~2 s) and the call returns

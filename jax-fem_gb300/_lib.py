@@ -98,6 +98,8 @@ SIGNATURES = {
     "fem_axpy_f32_f64": ([F64, P, P, I64, P], C.c_int),
     "fem_dot": ([I32, P, P, I64, P, P, SZ, P], C.c_int),
     "fem_selftest_bounded_wait": ([P, SZ, P], C.c_int),
+    "fem_spmv_timing_start": ([], C.c_int),
+    "fem_spmv_timing_stop": ([PF64, PI64], C.c_int),
     "fem_row_abs_sum": ([I64, P, P, F64, P, P], C.c_int),
     "fem_dr_march": ([I64, F64, P, P, P, P, P, P], C.c_int),
     "fem_dr_measure": ([I64, F64, F64, P, P, P, P, P, P, P, P, PF64, P, SZ, P], C.c_int),

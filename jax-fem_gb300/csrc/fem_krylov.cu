@@ -1855,9 +1855,43 @@ static void launch_spmv(const fem_pattern_t* pat, int64_t n_nodes, const T* vals
   launch_spmv_any<VEC, FMT>(pat, n_nodes, mfmt, vals, nullptr, x, nullptr, y, a, C, op, partials, nd, s);
 }
 
+// Optional in-solve timing of the mixed CG's SpMV (fem_spmv_timing_start / _stop): a CUDA event
+// pair around the first SpMV of every CHUNK-iteration chunk, on the solver's stream, read back
+// at the next poll (which has synchronised the stream).  Process-wide; not for concurrent solves.
+struct SpmvTimer {
+  bool on = false;
+  cudaEvent_t ev[2 * 64] = {};
+  int used = 0;          // pairs recorded since the last read-back
+  double seconds = 0.0;  // summed durations
+  int64_t samples = 0;
+};
+static SpmvTimer g_spmv_timer;
+
+static void spmv_timer_mark(int end, cudaStream_t s) {
+  SpmvTimer& T = g_spmv_timer;
+  if (!T.on || T.used >= 64) return;
+  cudaEvent_t& e = T.ev[2 * T.used + end];
+  if (!e && cudaEventCreate(&e) != cudaSuccess) { e = nullptr; T.on = false; return; }
+  cudaEventRecord(e, s);
+  if (end) ++T.used;
+}
+
+static void spmv_timer_collect() {
+  SpmvTimer& T = g_spmv_timer;
+  for (int k = 0; k < T.used; ++k) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, T.ev[2 * k], T.ev[2 * k + 1]) == cudaSuccess) {
+      T.seconds += 1e-3 * ms;
+      ++T.samples;
+    }
+  }
+  T.used = 0;
+}
+
 static int poll(KCtl* C, cudaStream_t s, KCtl* host) {
   FEM_CUDA(cudaMemcpyAsync(host, C, sizeof(KCtl), cudaMemcpyDeviceToHost, s));
   FEM_CUDA(cudaStreamSynchronize(s));
+  if (g_spmv_timer.used) spmv_timer_collect();
   if (host->fault) return fail(FEM_ERR_DEVICE, "a bounded device wait (bulk-copy barrier) ran out");
   return FEM_OK;
 }
@@ -2285,8 +2319,10 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
       }
       if (launched >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
       for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
+        if (k == 0) spmv_timer_mark(0, s);
         rc = launch_dfdf<VEC, SYM>(pat, n_nodes, vhi, vlo, pp, qh, ql, C, FIN_PCG_ALPHA, w.partials, s, qT);
         if (rc) return rc;
+        if (k == 0) spmv_timer_mark(1, s);
         if constexpr (VEC == 3) {
           if (SYM || !launch_update_bulk<PC>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C, w.partials,
                                              FIN_PCGR_UPDATE, s))
@@ -2571,6 +2607,26 @@ extern "C" int fem_axpy_f32_f64(double alpha, const float* x, double* y, int64_t
   if (n == 0) return FEM_OK;
   axpy_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(alpha, x, y, n);
   return check_launch("axpy");
+}
+
+extern "C" int fem_spmv_timing_start(void) {
+  g_spmv_timer.on = true;
+  g_spmv_timer.used = 0;
+  g_spmv_timer.seconds = 0.0;
+  g_spmv_timer.samples = 0;
+  return FEM_OK;
+}
+
+extern "C" int fem_spmv_timing_stop(double* seconds, int64_t* samples) {
+  FEM_REQUIRE(seconds && samples, "NULL argument");
+  if (g_spmv_timer.used) {
+    FEM_CUDA(cudaDeviceSynchronize());
+    spmv_timer_collect();
+  }
+  g_spmv_timer.on = false;
+  *seconds = g_spmv_timer.seconds;
+  *samples = g_spmv_timer.samples;
+  return FEM_OK;
 }
 
 extern "C" int fem_selftest_bounded_wait(void* ws, size_t ws_bytes, void* stream) {

@@ -45,6 +45,12 @@ def test_argument_errors_without_gpu(lib):
     with pytest.raises(jf._lib.FemError):
         jf._lib.call("fem_krylov_workspace", -1, jf._lib.FEM_F32, C.byref(nb))
     assert lib.fem_version() >= 100
+    # in-solve SpMV timing: nothing recorded without a solve; NULL outputs rejected
+    sec, cnt = C.c_double(-1.0), C.c_int64(-1)
+    assert lib.fem_spmv_timing_start() == jf._lib.FEM_OK
+    assert lib.fem_spmv_timing_stop(C.byref(sec), C.byref(cnt)) == jf._lib.FEM_OK
+    assert sec.value == 0.0 and cnt.value == 0
+    assert lib.fem_spmv_timing_stop(None, None) == jf._lib.FEM_ERR_ARG
 
 
 def test_widened_entry_points_validate_arguments(lib):
