@@ -195,7 +195,8 @@ def _newton_step(problem, eng, dofs, res, spec, precision, cfg):
             assert err < 0.1, f"linear solver failed to converge with err = {err}"
         inc = x
     elif spec.method == "cg":
-        # FP32 PCG with FP64 reliable updates: converges on the FP64 true residual
+        # PCG with FP64 reliable updates (double-float on the DF48 copy for 'mixed', FP32 for
+        # 'mixed32'): converges on the FP64 true residual
         x = x0.clone()
         it, up, rn, st = eng.pcg_refined(A, b, x, dofs, spec.pc, spec.rtol, spec.atol,
                                          cfg.get("refine_delta", 0.1), spec.maxiter)

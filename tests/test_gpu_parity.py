@@ -97,6 +97,19 @@ def test_cube_solution_gold_and_oracle(cuda):
     assert np.abs(sol - osol).max() <= 1e-7 * np.abs(osol).max()
 
 
+def test_mixed_bicgstab_newton_refinement(cuda):
+    """precision='mixed' with the reference's default jax_solver (BiCGStab + Jacobi): the
+    BiCGStab runs in FP32 on the sliced FP32 copy and Newton's FP64 residual refines it; at
+    rel_tol 1e-11 (the FP64 residual of this cube bottoms out near 2.5e-12) the solution matches
+    the oracle's direct solve to 1e-8 relative."""
+    import jax_fem_gb300 as jf
+    from oracle import solve as osolve
+    prob, oprob = _cube(cuda)
+    sol = jf.solver(prob, {"jax_solver": {}, "precision": "mixed", "rel_tol": 1e-11, "tol": 0.0})[0].cpu().numpy()
+    osol = osolve.newton_solve(oprob, {"spsolve_solver": {}})
+    assert np.abs(sol - osol).max() <= 1e-8 * np.abs(osol).max()
+
+
 def test_bicgstab_matches_jax_iteration(cuda):
     """fem_bicgstab follows jax.scipy's BiCGStab: same iteration count and iterate as the restated loop."""
     import jax_fem_gb300 as jf
@@ -138,6 +151,25 @@ def test_poisson_gold(cuda):
     prob, _ = cases.poisson(g)
     sol = jf.solver(prob)[0].cpu().numpy()
     np.testing.assert_array_almost_equal(g["sol"], sol, decimal=5)
+
+
+@pytest.mark.parametrize("pc", ["jacobi", "bjacobi", "none"])
+def test_poisson_mixed_vec1(cuda, pc):
+    """The mixed CG on a scalar problem (vec 1: the generic double-float update and direction
+    kernels, not the 32-node tiles): the Poisson gold fixture (decimal 5), the oracle's direct
+    solve (1e-9 relative) and the FP64 CG (1e-10), for each preconditioner."""
+    import cases
+    import jax_fem_gb300 as jf
+    from oracle import solve as osolve
+    g = golden("linear_poisson")
+    prob, oprob = cases.poisson(g)
+    lin = {"petsc_solver": {"ksp_type": "cg", "pc_type": pc, "rtol": 1e-12}, "rel_tol": 1e-12, "tol": 0.0}
+    s64 = jf.solver(prob, lin)[0].cpu().numpy()
+    smx = jf.solver(prob, dict(lin, precision="mixed"))[0].cpu().numpy()
+    np.testing.assert_array_almost_equal(g["sol"], smx, decimal=5)
+    osol = np.asarray(osolve.newton_solve(oprob, {"spsolve_solver": {}})).reshape(smx.shape)
+    assert np.abs(smx - osol).max() <= 1e-9 * np.abs(osol).max()
+    assert np.abs(smx - s64).max() <= 1e-10 * np.abs(s64).max()
 
 
 def test_cylinder_gold_and_area(cuda):
