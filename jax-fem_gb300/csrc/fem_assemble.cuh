@@ -9,8 +9,10 @@
 //      nodal u (and w) into shared memory                 (thread per cell node)
 //   B  geometry at each quadrature point: J, det, J^-1, physical shape grads,
 //      JxW; material stress/tangent pre-scaled by JxW    (thread per cell qp)
-//   C  element matrix rows K[(a,i),:] and atomic scatter into the CSR value
-//      slots given by the per-cell slot table             (thread per cell row)
+//   C  element matrix and atomic scatter into the CSR value slots given by the
+//      per-cell slot table: isotropic materials one 3x3 node-pair block a <= b
+//      and its transpose per item (item per cell node pair); otherwise rows
+//      K[(a,i),:]                                          (thread per cell row)
 //   D  element residual / tangent action rows, pre-reduced across the warp
 //      (lanes hitting the same dof are summed first), then FP64 atomics.
 #pragma once
@@ -252,42 +254,52 @@ cell_kernel(const AsmParams P) {
     const bool row_bc = active && P.bc && P.bc[row];
 
     if constexpr (TAN == TAN_ISO && VEC == 3) {
-      if (want_mat && active && !(row_bc && P.bc_mode != FEM_BC_NONE)) {
-        // K[(a,i),(b,k)] = sum_q lam g_a,i g_b,k + mu g_a,k g_b,i + mu (g_a . g_b) delta_ik, with
-        // this thread's three columns rotated so that m = 0 is k = i (k = (i + m) mod 3): the
-        // diagonal term then lands on a fixed accumulator and, with g_b,i = g_b,k there, the
-        // three m = 0 terms fold into one coefficient lam g_a,i + 2 mu g_a,i.  Seven FMAs per
-        // (qp, b); the three threads of node a no longer repeat a select-and-add per column.
-        const int i1 = i == 2 ? 0 : i + 1, i2 = i == 0 ? 2 : i - 1;
-        T acc[NN][3];
-        for (int b = 0; b < NN; ++b) acc[b][0] = acc[b][1] = acc[b][2] = T(0);
-        for (int q = 0; q < NQ; ++q) {
-          const T* G = sG + (c * NQ + q) * NN * 3;
-          const T* tq = sTan + (c * NQ + q) * NTAN;
-          const T lam = tq[0], mu = tq[1];
-          const T ga0 = G[a * 3 + i], ga1 = G[a * 3 + i1], ga2 = G[a * 3 + i2];
-          const T m0 = mu * ga0, m1 = mu * ga1, m2 = mu * ga2;
-          const T c0 = lam * ga0 + T(2) * m0;
-          const T l0 = lam * ga0;
-#pragma unroll
-          for (int b = 0; b < NN; ++b) {
-            const T gb0 = G[b * 3 + i], gb1 = G[b * 3 + i1], gb2 = G[b * 3 + i2];
-            acc[b][0] = fma(c0, gb0, fma(m1, gb1, fma(m2, gb2, acc[b][0])));
-            acc[b][1] = fma(l0, gb1, fma(m1, gb0, acc[b][1]));
-            acc[b][2] = fma(l0, gb2, fma(m2, gb0, acc[b][2]));
-          }
-        }
+      if (want_mat) {
+        // K[(a,i),(b,k)] = sum_q lam g_a,i g_b,k + mu g_a,k g_b,i + mu (g_a . g_b) delta_ik.  lam / mu
+        // = cr is the same at every point (only E varies), so with M_ab = sum_q mu g_a (x) g_b
+        //   K_ab = cr M_ab + M_ab^T + tr(M_ab) I,   K_ba = K_ab^T:
+        // one item per cell and node pair a <= b, 9 FMAs per quadrature point; the item scatters
+        // block (a, b) into node a's rows and, for a != b, its transpose into node b's rows.
+        constexpr int NP = NN * (NN + 1) / 2;
+        const T cr = Mat::lam_over_mu(P.mc);
         T* vals = reinterpret_cast<T*>(P.vals);
-        const int64_t rs = P.indptr[row];
-        const uint8_t* sl = P.slots + (e * NN + a) * NN;
-        const int kk[3] = {i, i1, i2};
-        for (int b = 0; b < NN; ++b) {
-          const int nb = sConn[c * NN + b];
-          T* dst = vals + rs + (int64_t)3 * sl[b];
+        for (int t = tid; t < CPB * NP; t += blockDim.x) {
+          const int cc = t / NP;
+          int pp = t - cc * NP, pa = 0;
+          while (pp >= NN - pa) { pp -= NN - pa; ++pa; }
+          const int pb = pa + pp;
+          const int64_t ee = tile * CPB + cc;
+          if (ee >= P.n_cells) continue;
+          T M[3][3] = {};
+          for (int q = 0; q < NQ; ++q) {
+            const T* G = sG + (cc * NQ + q) * NN * 3;
+            const T mu = sTan[(cc * NQ + q) * NTAN + 1];
+            const T m0 = mu * G[pa * 3], m1 = mu * G[pa * 3 + 1], m2 = mu * G[pa * 3 + 2];
+            const T g0 = G[pb * 3], g1 = G[pb * 3 + 1], g2 = G[pb * 3 + 2];
+            M[0][0] = fma(m0, g0, M[0][0]); M[0][1] = fma(m0, g1, M[0][1]); M[0][2] = fma(m0, g2, M[0][2]);
+            M[1][0] = fma(m1, g0, M[1][0]); M[1][1] = fma(m1, g1, M[1][1]); M[1][2] = fma(m1, g2, M[1][2]);
+            M[2][0] = fma(m2, g0, M[2][0]); M[2][1] = fma(m2, g1, M[2][1]); M[2][2] = fma(m2, g2, M[2][2]);
+          }
+          const T tr = M[0][0] + M[1][1] + M[2][2];
+          const int64_t na2 = sConn[cc * NN + pa], nb2 = sConn[cc * NN + pb];
+          const int sab = P.slots[(ee * NN + pa) * NN + pb], sba = P.slots[(ee * NN + pb) * NN + pa];
 #pragma unroll
-          for (int m = 0; m < 3; ++m) {
-            if (P.bc_mode == FEM_BC_SYMMETRIC && P.bc[(int64_t)nb * 3 + kk[m]]) continue;
-            atomicAdd(dst + kk[m], acc[b][m]);
+          for (int ii = 0; ii < 3; ++ii) {
+            const int64_t ra = na2 * 3 + ii;
+            const bool abc = P.bc && P.bc[ra];
+            T* dst_a = vals + P.indptr[ra] + 3 * sab;
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk) {
+              const int64_t rb = nb2 * 3 + kk;
+              const bool bbc = P.bc && P.bc[rb];
+              const T kv = fma(cr, M[ii][kk], M[kk][ii]) + (ii == kk ? tr : T(0));   // K_ab[ii][kk]
+              // K[(a,ii),(b,kk)]: row ra, column rb
+              if (!(abc && P.bc_mode != FEM_BC_NONE) && !(bbc && P.bc_mode == FEM_BC_SYMMETRIC))
+                atomicAdd(dst_a + kk, kv);
+              // K[(b,kk),(a,ii)] = K[(a,ii),(b,kk)]: row rb, column ra
+              if (pa != pb && !(bbc && P.bc_mode != FEM_BC_NONE) && !(abc && P.bc_mode == FEM_BC_SYMMETRIC))
+                atomicAdd(vals + P.indptr[rb] + 3 * sba + ii, kv);
+            }
           }
         }
       }

@@ -76,6 +76,8 @@ struct Material<FEM_MAT_LINEAR_ELASTIC, 3, T> {
     iso_stress(g, lam, mu, S);
     if (want_tan) { tan[0] = lam; tan[1] = mu; }
   }
+  // lam / mu = 2 nu / (1 - 2 nu): the same at every point
+  __device__ static T lam_over_mu(const MatConsts& mc) { return T(2) * T(mc.c[1]) / (T(1) - T(2) * T(mc.c[1])); }
   __device__ static void dparam(const T*, const MatConsts&, const double*, const double*, T*) {}
 };
 
@@ -100,6 +102,8 @@ struct Material<FEM_MAT_SIMP, 3, T> {
     iso_stress(g, lam, mu, S);
     if (want_tan) { tan[0] = lam; tan[1] = mu; }
   }
+  // lam / mu = 2 nu / (1 - 2 nu): only E varies with theta
+  __device__ static T lam_over_mu(const MatConsts& mc) { return T(2) * T(mc.c[2]) / (T(1) - T(2) * T(mc.c[2])); }
   // dS/dtheta
   __device__ static void dparam(const T g[9], const MatConsts& mc, const double* qp, const double*, T dS[9]) {
     const T dE = dmodulus(T(qp[0]), mc);
