@@ -432,6 +432,30 @@ def test_bounded_wait_reports_and_context_survives(cuda):
     assert np.abs(sol.cpu().numpy() - osol).max() <= 1e-9 * np.abs(osol).max()
 
 
+def test_spmv_timing_inside_mixed_solve(cuda):
+    """fem_spmv_timing_start/stop around a mixed solve: one timed SpMV per 16-iteration chunk,
+    each between 0 and 10 ms on this small case; nothing is timed once stopped."""
+    import ctypes
+    import cases
+    import jax_fem_gb300 as jf
+    lib = jf._lib.load()
+    prob, _, theta_np = cases.simp_box(12, 6, 3)
+    prob.set_params(torch.tensor(theta_np, device=cuda))
+    lin = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-10}, "precision": "mixed"}
+    sec, cnt = ctypes.c_double(), ctypes.c_int64()
+    assert lib.fem_spmv_timing_start() == jf._lib.FEM_OK
+    jf.solver(prob, lin)
+    assert lib.fem_spmv_timing_stop(ctypes.byref(sec), ctypes.byref(cnt)) == jf._lib.FEM_OK
+    its = sum(r["iterations"] for r in prob._engine.solve_log if r.get("iterations"))
+    assert cnt.value >= 1 and cnt.value <= its // 16 + 64
+    assert 0.0 < sec.value / cnt.value < 1e-2
+    first = (sec.value, cnt.value)
+    prob.set_params(torch.tensor(theta_np * 1.01, device=cuda))
+    jf.solver(prob, lin)
+    assert lib.fem_spmv_timing_stop(ctypes.byref(sec), ctypes.byref(cnt)) == jf._lib.FEM_OK
+    assert (sec.value, cnt.value) == first
+
+
 def test_maxiter_status(cuda):
     import cases
     import jax_fem_gb300 as jf
