@@ -82,7 +82,10 @@ enum {
   FEM_BC_SYMMETRIC = 2  /* skip Dirichlet rows and columns (symmetric elimination for CG) */
 };
 enum { FEM_PC_NONE = 0, FEM_PC_JACOBI = 1, FEM_PC_BJACOBI = 2 };
-enum { FEM_SOLVE_CONVERGED = 0, FEM_SOLVE_MAXITER = 1, FEM_SOLVE_BREAKDOWN = 2, FEM_SOLVE_NAN = 3 };
+/* FEM_SOLVE_STAGNATED (solvers with FP64 reliable updates): the FP64 true residual stopped falling
+ * above the target -- the attainable accuracy of the arithmetic; x holds the last iterate. */
+enum { FEM_SOLVE_CONVERGED = 0, FEM_SOLVE_MAXITER = 1, FEM_SOLVE_BREAKDOWN = 2, FEM_SOLVE_NAN = 3,
+       FEM_SOLVE_STAGNATED = 4 };
 
 /* ---- plain descriptor structs (pointers are device pointers) ------------- */
 typedef struct fem_mesh_t {

@@ -18,8 +18,8 @@ FEM_F32, FEM_F64, FEM_DF48, FEM_SLICED_F32, FEM_SLICED_F64, FEM_SLICED_DF48, FEM
 FEM_OUT_RESIDUAL, FEM_OUT_MATRIX, FEM_OUT_APPLY = 1, 2, 4
 FEM_BC_NONE, FEM_BC_ROWS, FEM_BC_SYMMETRIC = 0, 1, 2
 FEM_PC_NONE, FEM_PC_JACOBI, FEM_PC_BJACOBI = 0, 1, 2
-FEM_SOLVE_CONVERGED, FEM_SOLVE_MAXITER, FEM_SOLVE_BREAKDOWN, FEM_SOLVE_NAN = range(4)
-SOLVE_STATUS = {0: "converged", 1: "maxiter", 2: "breakdown", 3: "nan"}
+FEM_SOLVE_CONVERGED, FEM_SOLVE_MAXITER, FEM_SOLVE_BREAKDOWN, FEM_SOLVE_NAN, FEM_SOLVE_STAGNATED = range(5)
+SOLVE_STATUS = {0: "converged", 1: "maxiter", 2: "breakdown", 3: "nan", 4: "stagnated"}
 
 ELEM_IDS = {"HEX8": FEM_HEX8, "TET10": FEM_TET10, "TET4": FEM_TET4}
 

@@ -143,7 +143,11 @@ __device__ void finalize(KCtl* C, int op, const double (&d)[3], double* dot_out)
       C->iter += 1;
       C->rr = d[1];
       if (!finite(d[0]) || !finite(d[1])) { C->status = FEM_SOLVE_NAN; C->done = 1; break; }
-      if (d[1] <= C->check2 || d[1] <= C->delta2 * C->rmax2) { C->status = SOLVE_UPDATE; C->done = 1; break; }
+      // pause for an FP64 residual replacement: fallen by delta, below the target, or grown 1e4x
+      // (a recursive residual that far above its start is no longer trustworthy)
+      if (d[1] <= C->check2 || d[1] <= C->delta2 * C->rmax2 || d[1] > 1e8 * C->rmax2) {
+        C->status = SOLVE_UPDATE; C->done = 1; break;
+      }
       if (C->iter >= C->maxiter) { C->status = FEM_SOLVE_MAXITER; C->done = 1; break; }
       C->beta = d[0] / C->rho;
       C->rho = d[0];
@@ -1550,12 +1554,18 @@ __global__ void pcgx_direction_kernel(int64_t n_nodes, const float* z, float2* p
   }
 }
 
-// df <-> FP64 for the reliable updates: x64 = x (df) / scale ; (r.h, r.l) = split(r64 * scale).
+// df <-> FP64 for the reliable updates: (r.h, r.l) = split(r64 * scale), and the accumulation below.
 // scale is a power of two (exact both ways): it keeps the double-float vectors of a solve near
 // unit size, away from the ends of FP32's exponent range.
-__global__ void df_to_f64_kernel(int64_t n, const float* h, const float* l, double* out, double inv_scale) {
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    out[k] = ((double)h[k] + (double)l[k]) * inv_scale;
+// x64 += x (df) / scale ; x (df) := 0: a reliable update moves the correction that the double-float
+// iteration accumulated since the last update into the FP64 iterate, so the iterate itself keeps
+// FP64 precision (a 48-bit double-float iterate would floor the true residual near kappa * 2^-48)
+__global__ void df_accumulate_kernel(int64_t n, float* h, float* l, double* x64, double inv_scale) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    x64[k] += ((double)h[k] + (double)l[k]) * inv_scale;
+    h[k] = 0.f;
+    l[k] = 0.f;
+  }
 }
 __global__ void f64_to_df_kernel(int64_t n, const double* v, float* h, float* l, double scale) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
@@ -2132,6 +2142,8 @@ static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const flo
   if (rc) return rc;
   int64_t n_updates = 0;
   int final_status = FEM_SOLVE_CONVERGED;
+  double best_rr = h.rr_true;   // stagnation: three updates in a row without halving ||r_true||
+  int stalls = 0;
   const double delta2 = delta * delta;
   if (!(h.rr_true <= h.thresh2)) {
     // first start: z = M r, p = z
@@ -2156,6 +2168,8 @@ static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const flo
           if (h.rr_true <= h.thresh2) { final_status = FEM_SOLVE_CONVERGED; break; }
           if (!std::isfinite(h.rr_true)) { final_status = FEM_SOLVE_NAN; break; }
           if (h.iter >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
+          if (h.rr_true < 0.25 * best_rr) { best_rr = h.rr_true; stalls = 0; }
+          else if (++stalls >= 3) { final_status = FEM_SOLVE_STAGNATED; break; }
           pcgr_start_kernel<VEC, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, z, p, x32, pc, 0, C,
                                                                            w.partials);
           pcg_direction_kernel<float><<<vec_grid(n), VTHREADS, 0, s>>>(n, p, z, C);
@@ -2276,11 +2290,14 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
     scale = std::ldexp(1.0, -std::max(-900, std::min(900, e)));
   }
   const double inv_scale = 1.0 / scale;
-  f64_to_df_kernel<<<gv, VTHREADS, 0, s>>>(n, x, xh, xl, scale);
+  FEM_CUDA(cudaMemsetAsync(xh, 0, sizeof(float) * (size_t)n, s));   // the correction since the last update
+  FEM_CUDA(cudaMemsetAsync(xl, 0, sizeof(float) * (size_t)n, s));
   f64_to_df_kernel<<<gv, VTHREADS, 0, s>>>(n, r64, rh, rl, scale);
-  note_launches(2);
+  note_launches(1);
   int64_t n_updates = 0;
   int final_status = FEM_SOLVE_CONVERGED;
+  double best_rr = h.rr_true;   // stagnation: three updates in a row without halving ||r_true||
+  int stalls = 0;
   const double delta2 = delta * delta;
   const double check2 = h.check2 * scale * scale;   // the pause test runs on the scaled recursive residual
   if (!(h.rr_true <= h.thresh2)) {
@@ -2295,7 +2312,7 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
       if (h.done) {
         if (h.status == SOLVE_UPDATE || h.status == FEM_SOLVE_MAXITER) {
           const bool at_max = h.status == FEM_SOLVE_MAXITER;
-          df_to_f64_kernel<<<gv, VTHREADS, 0, s>>>(n, xh, xl, x, inv_scale);
+          df_accumulate_kernel<<<gv, VTHREADS, 0, s>>>(n, xh, xl, x, inv_scale);
           note_launches(1);
           rc = true_residual();
           if (rc) return rc;
@@ -2307,17 +2324,24 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
           if (h.rr_true <= h.thresh2) { final_status = FEM_SOLVE_CONVERGED; break; }
           if (!std::isfinite(h.rr_true)) { final_status = FEM_SOLVE_NAN; break; }
           if (at_max || h.iter >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
+          if (h.rr_true < 0.25 * best_rr) { best_rr = h.rr_true; stalls = 0; }
+          else if (++stalls >= 3) { final_status = FEM_SOLVE_STAGNATED; break; }
           pcgx_start_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, rh, rl, z, pp, pc, 0, C, w.partials);
           pcgx_direction_kernel<VEC><<<gn, VTHREADS, 0, s>>>(n_nodes, z, pp, C);
           note_launches(2);
           continue;
         }
         final_status = h.status;  // NaN or breakdown
-        df_to_f64_kernel<<<gv, VTHREADS, 0, s>>>(n, xh, xl, x, inv_scale);
+        df_accumulate_kernel<<<gv, VTHREADS, 0, s>>>(n, xh, xl, x, inv_scale);
         note_launches(1);
         break;
       }
-      if (launched >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
+      if (launched >= maxiter) {
+        final_status = FEM_SOLVE_MAXITER;
+        df_accumulate_kernel<<<gv, VTHREADS, 0, s>>>(n, xh, xl, x, inv_scale);
+        note_launches(1);
+        break;
+      }
       for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
         if (k == 0) spmv_timer_mark(0, s);
         rc = launch_dfdf<VEC, SYM>(pat, n_nodes, vhi, vlo, pp, qh, ql, C, FIN_PCG_ALPHA, w.partials, s, qT);
@@ -2386,6 +2410,8 @@ static int pcg_df_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* va
   if (rc) return rc;
   int64_t n_updates = 0;
   int final_status = FEM_SOLVE_CONVERGED;
+  double best_rr = h.rr_true;   // stagnation: three updates in a row without halving ||r_true||
+  int stalls = 0;
   const double delta2 = delta * delta;
   if (!(h.rr_true <= h.thresh2)) {
     FEM_CUDA(cudaMemcpyAsync(&C->delta2, &delta2, sizeof(double), cudaMemcpyHostToDevice, s));
@@ -2407,6 +2433,8 @@ static int pcg_df_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* va
           if (h.rr_true <= h.thresh2) { final_status = FEM_SOLVE_CONVERGED; break; }
           if (!std::isfinite(h.rr_true)) { final_status = FEM_SOLVE_NAN; break; }
           if (at_max || h.iter >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
+          if (h.rr_true < 0.25 * best_rr) { best_rr = h.rr_true; stalls = 0; }
+          else if (++stalls >= 3) { final_status = FEM_SOLVE_STAGNATED; break; }
           pcgd_start_kernel<VEC, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, z, p, phi, plo, pc, 0, C,
                                                                            w.partials);
           pcgd_direction_kernel<<<vec_grid(n), VTHREADS, 0, s>>>(n, p, z, phi, plo, C);
