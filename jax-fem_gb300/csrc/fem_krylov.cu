@@ -2092,9 +2092,11 @@ static int ref_apply(const fem_pattern_t* pat, int64_t n_nodes, const RefOp& op,
 // the FP32 matrix; whenever the FP32 recursive residual has fallen by `delta` since the
 // last replacement (or below a quarter of the target), the device pauses, the host adds
 // the FP32 increment into the FP64 solution and recomputes the true residual b - A x in
-// FP64 with the matrix-free tangent action (fem_assemble FEM_OUT_APPLY), which replaces
-// the FP32 residual.  The search direction is kept, so the Krylov recurrence continues
-// instead of restarting.  Convergence is declared only on the FP64 true residual.
+// FP64 (with the FP64 CSR tangent when given, else the matrix-free tangent action,
+// fem_assemble FEM_OUT_APPLY), which replaces the FP32 residual.  The search direction is
+// kept, so the Krylov recurrence continues instead of restarting.  Convergence is declared
+// only on the FP64 true residual; three replacements in a row that do not halve it end the
+// solve as stagnated.  r and the increment carry a power-of-two scale (see below).
 template <int VEC, int PC>
 static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const float* vals, const float* pc,
                             const RefOp& op, const double* b, double* x, double rtol, double atol, double delta,

@@ -5,9 +5,12 @@ Mirrors jax_fem/solver.py (Newton branch, 63-553 and 1079-1455):
   * solver_options has the same layout: a 'newton' block (or the legacy flat
     dict) with tol / rel_tol / line_search_flag / initial_guess and a 'linear'
     block naming jax_solver / petsc_solver / spsolve_solver / custom_solver.
-    Additional keys: 'precision' ('fp64' default, or 'mixed': FP32 tangent
-    and FP32 Krylov iterations inside FP64 Newton/refinement residuals),
-    'inner_rtol' (mixed inner tolerance), 'max_iter' (Newton cap).
+    Additional keys: 'precision' ('fp64' default; 'mixed': CG on a DF48 copy of
+    the FP64 tangent with double-float vectors and FP64 reliable updates;
+    'mixed_sym': the same on upper-block storage; 'mixed32': FP32 matrix and
+    vectors with FP64 reliable updates -- BiCGStab under a mixed precision runs
+    in FP32 and Newton's FP64 residual refines it), 'inner_rtol' (that
+    BiCGStab's tolerance), 'refine_delta', 'max_iter' (Newton cap).
   * jax_solver -> BiCGStab with jax.scipy's iteration and stopping rule on the
     row-eliminated matrix (solver.py:63-92), Jacobi if precond.
   * petsc_solver ksp_type 'cg' -> PCG on the symmetrically eliminated matrix
