@@ -21,6 +21,28 @@ def _declared():
     return names
 
 
+def _header_enums():
+    """Every `FEM_NAME = value` enumerator in include/*.h (comments stripped)."""
+    vals = {}
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", f)).read(), flags=re.S)
+            for body in re.findall(r"enum\s*\{(.*?)\}", src, flags=re.S):
+                for name, v in re.findall(r"\b(FEM_[A-Z0-9_]+)\s*=\s*(\d+)", body):
+                    vals[name] = int(v)
+    return vals
+
+
+def test_python_constants_match_header_enums():
+    """The ctypes layer's FEM_* constants equal the header's enumerators (no ABI drift)."""
+    import jax_fem_gb300 as jf
+    vals = _header_enums()
+    assert len(vals) >= 30 and vals["FEM_SOLVE_STAGNATED"] == 4
+    for name, v in vals.items():
+        assert getattr(jf._lib, name) == v, name
+    assert set(jf._lib.SOLVE_STATUS) == {v for k, v in vals.items() if k.startswith("FEM_SOLVE_")}
+
+
 def test_library_exports_every_declared_symbol(lib):
     names = _declared()
     assert len(names) >= 25
