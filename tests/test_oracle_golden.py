@@ -2,6 +2,7 @@
 tolerances (tests/benchmarks/*/test_*.py): decimal 5 (cube, Poisson, Neo-Hookean),
 decimal 3 (cylinder solution, J2 averaged stress), decimal 4 (cylinder area)."""
 import numpy as np
+import pytest
 import torch
 
 from conftest import golden
@@ -127,3 +128,48 @@ def test_oracle_adjoint_matches_fd():
             p.internal_vars = setp(p, torch.tensor(t2))
             vals.append(f @ solve.newton_solve(p, {"spsolve_solver": {}}).reshape(-1))
         assert abs((vals[0] - vals[1]) / (2 * h) - g[c, 0]) <= 1e-6 * np.abs(g).max()
+
+
+@pytest.mark.parametrize("ele", ["HEX8", "TET10", "TET4"])
+def test_isotropic_node_pair_tangent_identity(ele):
+    """The identity the assembly kernel's isotropic tangent rests on: for lam / mu the same at
+    every quadrature point (linear-elastic and SIMP materials; only E varies), the element block
+    sum_q JxW (lam g_a g_b^T + mu g_b g_a^T + mu (g_a . g_b) I) equals (lam/mu) M_ab + M_ab^T +
+    tr(M_ab) I with M_ab = sum_q JxW mu g_a g_b^T, and K_ba = K_ab^T.  Checked on a distorted
+    element with a different E at each point against B^T D B in Voigt form (1e-13)."""
+    from oracle import basis
+    rng = np.random.default_rng(7)
+    t = basis.element_tables(ele)
+    grads_ref, w = t["shape_grads_ref"], t["quad_weights"]
+    nq, nn, _ = grads_ref.shape
+    nu = 0.3
+    E = 1.0 + rng.random(nq)                                     # a different modulus per point
+    lam, mu = E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))
+    X = np.eye(3) + 0.2 * rng.standard_normal((3, 3))            # affine map of the reference cell
+    Kd = np.zeros((nn * 3, nn * 3))
+    Kp = np.zeros_like(Kd)
+    for q in range(nq):
+        G = grads_ref[q] @ np.linalg.inv(X)                      # physical gradients (nn, 3)
+        jxw = abs(np.linalg.det(X)) * w[q]
+        B = np.zeros((6, nn * 3))                                # Voigt strain-displacement matrix
+        for a in range(nn):
+            gx, gy, gz = G[a]
+            B[:, 3 * a:3 * a + 3] = [[gx, 0, 0], [0, gy, 0], [0, 0, gz],
+                                     [gy, gx, 0], [0, gz, gy], [gz, 0, gx]]
+        D = np.zeros((6, 6))
+        D[:3, :3] = lam[q]
+        D[:3, :3] += 2 * mu[q] * np.eye(3)
+        D[3:, 3:] = mu[q] * np.eye(3)
+        Kd += jxw * B.T @ D @ B
+        for a in range(nn):
+            for b in range(nn):
+                Kp[3 * a:3 * a + 3, 3 * b:3 * b + 3] += jxw * mu[q] * np.outer(G[a], G[b])
+    cr = 2 * nu / (1 - 2 * nu)
+    Kn = np.zeros_like(Kd)
+    for a in range(nn):
+        for b in range(a, nn):
+            M_ab = Kp[3 * a:3 * a + 3, 3 * b:3 * b + 3]
+            K_ab = cr * M_ab + M_ab.T + np.trace(M_ab) * np.eye(3)
+            Kn[3 * a:3 * a + 3, 3 * b:3 * b + 3] = K_ab
+            Kn[3 * b:3 * b + 3, 3 * a:3 * a + 3] = K_ab.T
+    assert np.abs(Kn - Kd).max() <= 1e-13 * np.abs(Kd).max()
