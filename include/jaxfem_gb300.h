@@ -232,6 +232,12 @@ int fem_zero_rows(const fem_pattern_t* pat, int32_t vec, int32_t precision, void
                   const int32_t* rows, int64_t n_rows, double diag_value, void* stream);
 int fem_apply_bc_vec(double* res, const double* dofs, const int32_t* rows, const double* values,
                      int64_t n_rows, double scale, void* stream);
+/* fem_matrix_transpose: vals_t := A^T in the same CSR pattern (out of place; FP32 / FP64 CSR
+ * order).  Replaces the PETSc transpose of the adjoint (solver.py:1405-1409: A_T =
+ * A.transpose(); the adjoint solves A_T lam = v).  ws: >= 4 bytes of device scratch (a pattern
+ * error flag).  Fails with FEM_ERR_ARG if a block (I, J) has no (J, I) partner.  Syncs. */
+int fem_matrix_transpose(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
+                         const void* vals, void* vals_t, void* ws, size_t ws_bytes, void* stream);
 
 /* ---- sparse linear algebra ------------------------------------------------
  * Replaces jax.scipy.sparse.linalg.bicgstab on the BCOO matrix (solver.py:63-92)
@@ -276,14 +282,19 @@ int fem_pcg(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t prec
             double rtol, double atol, int64_t maxiter, void* ws, size_t ws_bytes,
             int64_t* iterations, double* res_norm, int32_t* status, void* stream);
 /* Allocation-free PCG (no counterpart in the reference).  Same method, arguments and result
- * as fem_pcg, for callers that cannot allocate device memory: code running while a stream is
- * captured into a CUDA graph, host frameworks whose allocator is closed to plug-ins, embeddings
- * that forbid allocation after start-up.  Its scratch is a fixed file-scope device array of
+ * as fem_pcg, for callers that cannot allocate device memory: host frameworks whose device
+ * allocator is closed to plug-ins, and embeddings that reserve all device memory up front and
+ * forbid allocation after start-up.  Its scratch is a fixed file-scope device array of
  * about 8.6 MB that every GPU loading the library keeps until the process exits; systems of
  * more than 262144 dofs (n_nodes*vec) are rejected with FEM_ERR_CAPACITY.  The first call on a
- * device looks up the array's device address (make that first call before any stream capture).
+ * device looks up the array's device address and caches it for that device (make that first
+ * call before any stream capture).  The cached address belongs to the CUDA context of that
+ * first call: after cudaDeviceReset on a device, the next call would hand the kernels a stale
+ * address, so a process that resets a device must not call this entry point on it again.
  * Every call shares the array, so calls that overlap on the GPU (two streams, two threads)
- * race: serialise them.  Allocates nothing (no cudaMalloc / cudaFree).  Syncs. */
+ * race: serialise them.  Allocates nothing (no cudaMalloc / cudaFree).  Like fem_pcg it
+ * synchronises with the host while it runs: it reads the convergence flag back every 16
+ * iterations. */
 int fem_pcg_static(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
                    const void* vals, int32_t pc_kind, const void* pc, const void* b, void* x,
                    double rtol, double atol, int64_t maxiter, int64_t* iterations, double* res_norm,

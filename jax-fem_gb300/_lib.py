@@ -80,6 +80,7 @@ SIGNATURES = {
     "fem_j2_history_vjp": ([PMESH, PMAT, P, P, P, P, P, P, P, P], C.c_int),
     "fem_zero_rows": ([PPAT, I32, I32, P, P, I64, F64, P], C.c_int),
     "fem_apply_bc_vec": ([P, P, P, P, I64, F64, P], C.c_int),
+    "fem_matrix_transpose": ([PPAT, I64, I32, I32, P, P, P, SZ, P], C.c_int),
     "fem_spmv": ([PPAT, I64, I32, I32, P, P, P, P], C.c_int),
     "fem_precond_setup": ([PPAT, I64, I32, I32, P, I32, P, P], C.c_int),
     "fem_krylov_workspace": ([I64, I32, PSZ], C.c_int),

@@ -1708,6 +1708,37 @@ __global__ void zero_rows_kernel(int vec, const int64_t* bp, const int64_t* indp
   }
 }
 
+// A^T in the same node-block CSR pattern (the pattern is structurally symmetric: the union of
+// every cell's dof pairs).  Thread per node row I: for each block (I, J) it finds block (J, I) in
+// row J by binary search and writes the transposed block, value (r, d) of (I, J) := value (d, r)
+// of (J, I).  Rows are independent, so the output needs no atomics.
+template <typename T>
+__global__ void transpose_kernel(int vec, int64_t n_nodes, const int64_t* __restrict__ bp,
+                                 const int32_t* __restrict__ bcols, const T* __restrict__ v, T* __restrict__ vt,
+                                 int* __restrict__ err) {
+  GRID_STRIDE_NODES(I, n_nodes) {
+    const int64_t bI = bp[I];
+    const int nI = (int)(bp[I + 1] - bI);
+    for (int k = 0; k < nI; ++k) {
+      const int64_t J = bcols[bI + k];
+      const int64_t bJ = bp[J];
+      const int nJ = (int)(bp[J + 1] - bJ);
+      int lo = 0, hi = nJ - 1, kt = -1;
+      while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int64_t c = bcols[bJ + mid];
+        if (c == I) { kt = mid; break; }
+        if (c < I) lo = mid + 1; else hi = mid - 1;
+      }
+      if (kt < 0) { atomicExch(err, 1); continue; }   // pattern not structurally symmetric
+      for (int r = 0; r < vec; ++r)
+        for (int d = 0; d < vec; ++d)
+          vt[(int64_t)vec * vec * bI + (int64_t)r * vec * nI + vec * k + d] =
+              v[(int64_t)vec * vec * bJ + (int64_t)d * vec * nJ + vec * kt + r];
+    }
+  }
+}
+
 __global__ void apply_bc_vec_kernel(double* res, const double* dofs, const int32_t* rows, const double* values,
                                     int64_t n, double scale) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
@@ -2095,8 +2126,15 @@ static int ref_apply(const fem_pattern_t* pat, int64_t n_nodes, const RefOp& op,
 // FP64 (with the FP64 CSR tangent when given, else the matrix-free tangent action,
 // fem_assemble FEM_OUT_APPLY), which replaces the FP32 residual.  The search direction is
 // kept, so the Krylov recurrence continues instead of restarting.  Convergence is declared
-// only on the FP64 true residual; three replacements in a row that do not halve it end the
-// solve as stagnated.  r and the increment carry a power-of-two scale (see below).
+// only on the FP64 true residual; three replacements in a row that do not cut it by
+// stall_factor(delta) end the solve as stagnated.  r and the increment carry a power-of-two scale (see below).
+// Progress an FP64 residual replacement must show to reset the stagnation count: the squared
+// true residual below this fraction of the best so far.  A healthy replacement follows a pause
+// of the recursive residual at delta^2 of its start, so it cuts the squared true residual by
+// about delta^2; the fraction max(1/4, delta) sits above that for every delta in (0, 1) and is
+// the plain "halve the norm" rule for delta <= 1/4.
+static inline double stall_factor(double delta) { return std::max(0.25, delta); }
+
 template <int VEC, int PC>
 static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const float* vals, const float* pc,
                             const RefOp& op, const double* b, double* x, double rtol, double atol, double delta,
@@ -2144,7 +2182,7 @@ static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const flo
   if (rc) return rc;
   int64_t n_updates = 0;
   int final_status = FEM_SOLVE_CONVERGED;
-  double best_rr = h.rr_true;   // stagnation: three updates in a row without halving ||r_true||
+  double best_rr = h.rr_true;   // stagnation: three updates in a row without progress (stall_factor)
   int stalls = 0;
   const double delta2 = delta * delta;
   if (!(h.rr_true <= h.thresh2)) {
@@ -2170,7 +2208,7 @@ static int pcg_refined_impl(const fem_pattern_t* pat, int64_t n_nodes, const flo
           if (h.rr_true <= h.thresh2) { final_status = FEM_SOLVE_CONVERGED; break; }
           if (!std::isfinite(h.rr_true)) { final_status = FEM_SOLVE_NAN; break; }
           if (h.iter >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
-          if (h.rr_true < 0.25 * best_rr) { best_rr = h.rr_true; stalls = 0; }
+          if (h.rr_true < stall_factor(delta) * best_rr) { best_rr = h.rr_true; stalls = 0; }
           else if (++stalls >= 3) { final_status = FEM_SOLVE_STAGNATED; break; }
           pcgr_start_kernel<VEC, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, z, p, x32, pc, 0, C,
                                                                            w.partials);
@@ -2298,7 +2336,7 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
   note_launches(1);
   int64_t n_updates = 0;
   int final_status = FEM_SOLVE_CONVERGED;
-  double best_rr = h.rr_true;   // stagnation: three updates in a row without halving ||r_true||
+  double best_rr = h.rr_true;   // stagnation: three updates in a row without progress (stall_factor)
   int stalls = 0;
   const double delta2 = delta * delta;
   const double check2 = h.check2 * scale * scale;   // the pause test runs on the scaled recursive residual
@@ -2326,7 +2364,7 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
           if (h.rr_true <= h.thresh2) { final_status = FEM_SOLVE_CONVERGED; break; }
           if (!std::isfinite(h.rr_true)) { final_status = FEM_SOLVE_NAN; break; }
           if (at_max || h.iter >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
-          if (h.rr_true < 0.25 * best_rr) { best_rr = h.rr_true; stalls = 0; }
+          if (h.rr_true < stall_factor(delta) * best_rr) { best_rr = h.rr_true; stalls = 0; }
           else if (++stalls >= 3) { final_status = FEM_SOLVE_STAGNATED; break; }
           pcgx_start_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, rh, rl, z, pp, pc, 0, C, w.partials);
           pcgx_direction_kernel<VEC><<<gn, VTHREADS, 0, s>>>(n_nodes, z, pp, C);
@@ -2412,7 +2450,7 @@ static int pcg_df_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* va
   if (rc) return rc;
   int64_t n_updates = 0;
   int final_status = FEM_SOLVE_CONVERGED;
-  double best_rr = h.rr_true;   // stagnation: three updates in a row without halving ||r_true||
+  double best_rr = h.rr_true;   // stagnation: three updates in a row without progress (stall_factor)
   int stalls = 0;
   const double delta2 = delta * delta;
   if (!(h.rr_true <= h.thresh2)) {
@@ -2435,7 +2473,7 @@ static int pcg_df_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* va
           if (h.rr_true <= h.thresh2) { final_status = FEM_SOLVE_CONVERGED; break; }
           if (!std::isfinite(h.rr_true)) { final_status = FEM_SOLVE_NAN; break; }
           if (at_max || h.iter >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
-          if (h.rr_true < 0.25 * best_rr) { best_rr = h.rr_true; stalls = 0; }
+          if (h.rr_true < stall_factor(delta) * best_rr) { best_rr = h.rr_true; stalls = 0; }
           else if (++stalls >= 3) { final_status = FEM_SOLVE_STAGNATED; break; }
           pcgd_start_kernel<VEC, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, z, p, phi, plo, pc, 0, C,
                                                                            w.partials);
@@ -2527,6 +2565,34 @@ extern "C" int fem_zero_rows(const fem_pattern_t* pat, int32_t vec, int32_t prec
                                                                    (double*)vals, rows, n_rows, diag_value);
   note_launches(1);
   return check_launch("zero_rows");
+}
+
+extern "C" int fem_matrix_transpose(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t precision,
+                                    const void* vals, void* vals_t, void* ws, size_t ws_bytes, void* stream) {
+  FEM_REQUIRE(pat && pat->block_ptr && pat->block_cols && vals && vals_t, "pattern/vals NULL");
+  FEM_REQUIRE(vals != vals_t, "fem_matrix_transpose works out of place");
+  FEM_REQUIRE(precision == FEM_F32 || precision == FEM_F64, "fem_matrix_transpose works on CSR-order FP32/FP64 values");
+  FEM_REQUIRE(vec == 1 || vec == 3, "vec must be 1 or 3");
+  FEM_REQUIRE(n_nodes >= 0, "n_nodes < 0");
+  FEM_REQUIRE(ws && ws_bytes >= sizeof(int), "workspace of at least 4 bytes required (error flag)");
+  if (n_nodes == 0) return FEM_OK;
+  cudaStream_t s = as_stream(stream);
+  int* err = static_cast<int*>(ws);
+  FEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+  if (precision == FEM_F32)
+    transpose_kernel<float><<<grid_for(n_nodes, 128), 128, 0, s>>>(vec, n_nodes, pat->block_ptr, pat->block_cols,
+                                                                   (const float*)vals, (float*)vals_t, err);
+  else
+    transpose_kernel<double><<<grid_for(n_nodes, 128), 128, 0, s>>>(vec, n_nodes, pat->block_ptr, pat->block_cols,
+                                                                    (const double*)vals, (double*)vals_t, err);
+  note_launches(1);
+  int rc = check_launch("matrix_transpose");
+  if (rc) return rc;
+  int h = 0;
+  FEM_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FEM_CUDA(cudaStreamSynchronize(s));
+  if (h) return fail(FEM_ERR_ARG, "fem_matrix_transpose: the block pattern is not structurally symmetric");
+  return FEM_OK;
 }
 
 extern "C" int fem_apply_bc_vec(double* res, const double* dofs, const int32_t* rows, const double* values,
@@ -2836,13 +2902,13 @@ extern "C" int fem_spmv_dfx(const fem_pattern_t* pat, int64_t n_nodes, int32_t v
 }
 
 // ---- allocation-free PCG ----------------------------------------------------------
-// For callers that cannot allocate device memory themselves -- code running while a
-// stream is being captured into a CUDA graph (allocation calls are not capturable), a
-// host framework whose allocator is closed to plug-ins, or an embedding that forbids
-// runtime allocation after start-up -- fem_pcg_static runs the same PCG as fem_pcg with
-// its scratch (control block, per-CTA partial sums, four Krylov vectors) in this
-// file-scope device array.  Every GPU that loads the library holds the array until the
-// process exits; every call shares it.
+// For callers that cannot allocate device memory themselves -- a host framework whose
+// device allocator is closed to plug-ins, or an embedding that reserves device memory up
+// front and forbids allocation after start-up -- fem_pcg_static runs the same PCG as
+// fem_pcg with its scratch (control block, per-CTA partial sums, four Krylov vectors) in
+// this file-scope device array.  Every GPU that loads the library holds the array until
+// the process exits; every call shares it, so calls that overlap on the GPU race.  Like
+// fem_pcg, it reads the convergence flag back to the host every 16 iterations.
 namespace fem {
 constexpr int64_t STATIC_PCG_MAX_DOFS = 262144;
 constexpr size_t al_c(size_t x) { return (x + 255) & ~size_t(255); }
@@ -2850,9 +2916,11 @@ constexpr size_t STATIC_PCG_BYTES = al_c(sizeof(KCtl)) + al_c(sizeof(double) * 3
                                     4 * al_c(sizeof(double) * STATIC_PCG_MAX_DOFS);
 __device__ __align__(256) unsigned char g_static_pcg_scratch[STATIC_PCG_BYTES];
 
-// Device address of the scratch array on the current device, looked up once per device.
-// The host-side name g_static_pcg_scratch is only a stand-in for the symbol and is never
-// passed to a kernel.
+// Device address of the scratch array on the current device, looked up once per device
+// (on the first call there, which should come before any stream capture).  The host-side
+// name g_static_pcg_scratch is only a stand-in for the symbol and is never passed to a
+// kernel.  The cached address belongs to the context of that first call; it is not
+// looked up again, so it does not survive a cudaDeviceReset of the device.
 static int static_pcg_scratch(void** out) {
   static std::mutex mu;
   static void* addr[128] = {};

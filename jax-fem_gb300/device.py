@@ -84,6 +84,17 @@ class DeviceCSR:
 
     __matmul__ = matvec
 
+    def transpose(self):
+        """A^T in the same CSR pattern (FP32 / FP64 CSR order), as the reference's PETSc
+        A.transpose() before the adjoint solve (solver.py:1405-1409)."""
+        if self.precision not in (_lib.FEM_F32, _lib.FEM_F64):
+            raise ValueError("transpose() works on FP32 / FP64 CSR matrices")
+        out = torch.empty_like(self.data)
+        ws = self.eng.workspace(_lib.FEM_F64)
+        call("fem_matrix_transpose", C.byref(self.eng.pattern), self.eng.num_nodes, self.eng.vec, self.precision,
+             ptr(self.data), ptr(out), ptr(ws), ws.numel(), _stream())
+        return DeviceCSR(self.eng, self.precision, out, self.bc_mode)
+
     @property
     def vector_dtype(self):
         return torch.float32 if self.precision in (_lib.FEM_F32, _lib.FEM_SLICED_F32) else torch.float64
@@ -163,6 +174,7 @@ class Engine:
                                  self.coords.data_ptr(), self.conn.data_ptr())
         self._build_pattern()
         self._bc_seen = None
+        self.bc_value_terms = []
         self._mat = None
         self._mat_key = None
         self._qp = None
@@ -255,17 +267,32 @@ class Engine:
         key = (fe.bc_version, id(fe.node_inds_list), id(fe.vals_list))
         if key == self._bc_seen:
             return
-        rows, vals = [], []
+        rows, vals, graph = [], [], []
         for n, v, val in zip(fe.node_inds_list, fe.vec_inds_list, fe.vals_list):
             rows.append(np.asarray(n, dtype=np.int64) * fe.vec + np.asarray(v, dtype=np.int64))
+            if torch.is_tensor(val):
+                if val.requires_grad:
+                    graph.append((len(vals), val))
+                val = val.detach().cpu().numpy()
             vals.append(np.asarray(val, dtype=np.float64))
+        # Dirichlet values that carry a torch graph (differentiable set_params): (positions in
+        # the final bc_rows, tensor entries) -- the adjoint sends lam_b to them
+        self.bc_value_terms = []
         if rows:
+            offs = np.concatenate([[0], np.cumsum([len(r) for r in rows])])
             rows = np.concatenate(rows)
             vals = np.concatenate(vals)
             # later lists overwrite earlier ones on shared rows (solver.py:297-300): keep the last
             _, last = np.unique(rows[::-1], return_index=True)
             keep = np.sort(len(rows) - 1 - last)
             rows, vals = rows[keep], vals[keep]
+            for li, t in graph:
+                c = np.arange(offs[li], offs[li + 1])
+                kept = np.isin(c, keep)
+                if kept.any():
+                    pos = np.searchsorted(keep, c[kept])
+                    self.bc_value_terms.append((torch.as_tensor(pos, device=self.device),
+                                                t[torch.as_tensor(np.nonzero(kept)[0], device=t.device)]))
         else:
             rows, vals = np.zeros(0, dtype=np.int64), np.zeros(0)
         dev = self.device
@@ -279,6 +306,12 @@ class Engine:
         self.n_bc = len(rows)
         self._bc_seen = key
         self._tangent_cache.clear()
+
+    @property
+    def tangent_symmetric(self):
+        """Whether K(u) is symmetric: the material's tangent (Robin parts are symmetric)."""
+        m, _ = self.material()
+        return bool(m.symmetric)
 
     # ---- external loads (mass / surface maps independent of u) -----------------------
     def refresh_loads(self):

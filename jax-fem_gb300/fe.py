@@ -58,6 +58,29 @@ def eval_pointwise(fn, args, out_shape_tail=()):
     return np.stack([single(p).reshape(tuple(out_shape_tail)) for p in range(P)])
 
 
+def _bc_values(fn, pts):
+    """Dirichlet values value_fn(point) at the BC nodes (fe.py:241-253).  A value function that
+    returns torch tensors (set_params closing over a parameter tensor, as in the reference's
+    compute_gradients example) gives a torch FP64 tensor that keeps any graph, so the adjoint
+    can send lam_b back to the parameter; otherwise a numpy array."""
+    v0 = fn(pts[0])
+    if torch.is_tensor(v0):
+        try:   # one call with the point axis last, checked against per-point calls
+            vv = fn(np.moveaxis(pts, 0, -1))
+            vv = torch.as_tensor(vv, dtype=torch.float64)
+            if vv.numel() == 1:
+                vv = vv.reshape(1).expand(len(pts))
+            elif vv.shape != (len(pts),):
+                raise ValueError
+            probe = np.unique(np.linspace(0, len(pts) - 1, min(len(pts), 5)).astype(np.int64))
+            if not all(abs(float(vv[p]) - float(fn(pts[p]))) <= 1e-12 * (abs(float(vv[p])) + 1.0) for p in probe):
+                raise ValueError
+            return vv.to(torch.float64)
+        except Exception:  # noqa: BLE001 -- per point
+            return torch.stack([torch.as_tensor(fn(p), dtype=torch.float64).reshape(()) for p in pts])
+    return np.asarray(eval_pointwise(fn, [pts]).reshape(-1), dtype=np.float64)
+
+
 def eval_location(fn, points):
     n = _nargs(fn)
     if n == 1:
@@ -122,11 +145,10 @@ class FiniteElement:
                 flags = eval_location(location_fns[i], self.points)
                 node_inds = np.argwhere(flags).reshape(-1)
                 vec_inds = np.ones_like(node_inds, dtype=np.int32) * vecs[i]
-                values = eval_pointwise(value_fns[i], [self.points[node_inds]]).reshape(-1) \
-                    if len(node_inds) else np.zeros(0)
+                values = _bc_values(value_fns[i], self.points[node_inds]) if len(node_inds) else np.zeros(0)
                 node_inds_list.append(node_inds)
                 vec_inds_list.append(vec_inds)
-                vals_list.append(np.asarray(values, dtype=np.float64))
+                vals_list.append(values)
         self.bc_version = getattr(self, "bc_version", 0) + 1
         return node_inds_list, vec_inds_list, vals_list
 

@@ -148,63 +148,59 @@ def _flat(sol_list, device):
 def _surface_map_split(fn, x, vec, max_degree=4):
     """Split a surface map t(u, x) into h(x) = t(0, x) at the face quadrature points and, when t
     depends on u, component-wise polynomial coefficients c[v][k] (k = 0..deg, c[v][0] = 0) with
-    t_v(u, x) = h_v(x) + sum_k c[v][k] u_v^k, found by probing and verified on random u.  Other
-    u-dependence raises NotImplementedError.  Returns (h flat, coeffs (vec, deg+1) or None)."""
+    t_v(u, x) = h_v(x) + sum_k c[v][k] u_v^k.  Every probe is evaluated at every face quadrature
+    point (one vectorised call where the map allows it), so u-dependence confined to part of the
+    boundary is still seen.  Other u-dependence raises NotImplementedError.
+    Returns (h flat, coeffs (vec, deg+1) or None)."""
     P = len(x)
-    h = eval_pointwise(lambda u, xx: fn(u, xx), [np.zeros((P, vec)), x], (vec,)).reshape(P, vec)
+    ev = lambda u: eval_pointwise(lambda uu, xx: fn(uu, xx), [u, x], (vec,)).reshape(P, vec)
+    h = ev(np.zeros((P, vec)))
     rng = np.random.default_rng(7)
-    probe = rng.integers(0, P, size=min(P, 3))
-    t = lambda u, p: np.asarray(fn(np.asarray(u, dtype=np.float64), x[p]), dtype=np.float64).reshape(vec)
-    if all(np.allclose(t(rng.standard_normal(vec), p), h[p], rtol=1e-12, atol=1e-12 * (np.abs(h[p]).max() + 1.0))
-           for p in probe):
+    tol = lambda ref: 1e-12 * (np.abs(ref).max(axis=-1, keepdims=True) + 1.0)
+    if np.all(np.abs(ev(rng.standard_normal((P, vec))) - h) <= tol(h)):
         return h.reshape(-1), None
     samples = np.array([-1.0, -0.5, 0.5, 1.0, 1.5, 2.0])
     V = samples[:, None] ** np.arange(1, max_degree + 1)[None, :]
     coeffs = np.zeros((vec, max_degree + 1))
     for v in range(vec):
-        fits = []
-        for p in probe:
-            rows = []
-            for sv in samples:
-                u = np.zeros(vec)
-                u[v] = sv
-                tv = t(u, p) - h[p]
-                others = np.delete(tv, v)
-                if not np.allclose(others, 0.0, atol=1e-12 * (np.abs(tv).max() + 1.0)):
-                    raise NotImplementedError("u-dependent surface maps must act component-wise")
-                rows.append(tv[v])
-            c, *_ = np.linalg.lstsq(V, np.array(rows), rcond=None)
-            fits.append(c)
-        fits = np.array(fits)
-        if not np.allclose(fits, fits[0], rtol=1e-9, atol=1e-12 * (np.abs(fits).max() + 1.0)):
+        rows = np.empty((len(samples), P))
+        for k, sv in enumerate(samples):
+            u = np.zeros((P, vec))
+            u[:, v] = sv
+            tv = ev(u) - h
+            others = np.delete(tv, v, axis=1)
+            if not np.all(np.abs(others) <= 1e-12 * (np.abs(tv).max(axis=1, keepdims=True) + 1.0)):
+                raise NotImplementedError("u-dependent surface maps must act component-wise")
+            rows[k] = tv[:, v]
+        fits, *_ = np.linalg.lstsq(V, rows, rcond=None)          # (max_degree, P): one fit per point
+        ref = fits[:, :1]
+        if not np.all(np.abs(fits - ref) <= 1e-9 * np.abs(ref) + 1e-12 * (np.abs(fits).max() + 1.0)):
             raise NotImplementedError("the u-dependent part of a surface map must not depend on x")
-        coeffs[v, 1:] = fits[0]
+        coeffs[v, 1:] = ref[:, 0]
     scale = np.abs(coeffs).max()
     if scale == 0.0:
         raise NotImplementedError("u-dependent surface maps must act component-wise")
     coeffs[np.abs(coeffs) <= 1e-13 * scale] = 0.0
     deg = max(int(np.nonzero(np.abs(coeffs).max(0))[0].max()), 1)
     coeffs = coeffs[:, :deg + 1]
-    for p in probe:
-        u = rng.uniform(-1.5, 1.5, vec)
-        pred = h[p] + np.array([np.polyval(coeffs[v][::-1], u[v]) for v in range(vec)])
-        if not np.allclose(t(u, p), pred, rtol=1e-9, atol=1e-11 * (np.abs(pred).max() + 1.0)):
-            raise NotImplementedError("only component-wise polynomial u-dependence (degree <= 4) is built for "
-                                      "surface maps")
+    u = rng.uniform(-1.5, 1.5, (P, vec))
+    pred = h + np.stack([np.polyval(coeffs[v][::-1], u[:, v]) for v in range(vec)], axis=1)
+    if not np.all(np.abs(ev(u) - pred) <= 1e-9 * np.abs(pred) + 1e-11 * (np.abs(pred).max(axis=1, keepdims=True) + 1.0)):
+        raise NotImplementedError("only component-wise polynomial u-dependence (degree <= 4) is built for "
+                                  "surface maps")
     logger.debug("surface map: u-dependent part of degree %d", deg)
     return h.reshape(-1), coeffs
 
 
 def _u_independent(fn, x, vec, what):
-    """Evaluate map(u, x) at points with u = 0 and check that it does not depend on u."""
+    """Evaluate map(u, x) at every point with u = 0 and check, again at every point, that a
+    random u gives the same value (a map whose u-dependence is confined to part of the domain
+    is refused, not integrated as a constant load)."""
     P = len(x)
-    u0 = np.zeros((P, vec))
-    val = eval_pointwise(lambda u, xx: fn(u, xx), [u0, x], (vec,))
+    val = eval_pointwise(lambda u, xx: fn(u, xx), [np.zeros((P, vec)), x], (vec,)).reshape(P, vec)
     rng = np.random.default_rng(7)
-    probe = rng.integers(0, P, size=min(P, 4))
-    for p in probe:
-        alt = np.asarray(fn(rng.standard_normal(vec), x[p]), dtype=np.float64).reshape(vec)
-        if not np.allclose(alt, val[p], rtol=1e-12, atol=1e-12 * (np.abs(val[p]).max() + 1.0)):
-            raise NotImplementedError(f"{what} depends on u; only u-independent {what}s are built")
+    alt = eval_pointwise(lambda u, xx: fn(u, xx), [rng.standard_normal((P, vec)), x], (vec,)).reshape(P, vec)
+    if not np.all(np.abs(alt - val) <= 1e-12 * np.abs(val) + 1e-12 * (np.abs(val).max(axis=1, keepdims=True) + 1.0)):
+        raise NotImplementedError(f"{what} depends on u; only u-independent {what}s are built")
     logger.debug("%s evaluated at %d points", what, P)
     return val.reshape(-1)

@@ -314,8 +314,13 @@ def _flat_v(v_list, device):
 
 def adjoint_solve(problem, dofs, v, adjoint_solver_options=None, precision="fp64", inner_rtol=1e-5,
                   max_refine=30):
-    """lam_f = K_ff^-1 v_f (the free block of A^T lam = v, solver.py:1399-1409).  Dirichlet
-    entries of lam are returned as 0: the parameter VJP never reads them.
+    """lam_f = K_ff^-T v_f (the free block of A^T lam = v, solver.py:1399-1409).  Dirichlet
+    entries of lam are returned as 0 (lam_b = v_b - K_fb^T lam_f is formed by
+    dirichlet_adjoint when a Dirichlet value is differentiated).
+
+    A non-symmetric tangent (GeneralLinear with C != C^T) is transposed on the device
+    (fem_matrix_transpose, the reference's A.transpose()) and solved in FP64 whatever the
+    precision; symmetric tangents solve K_ff itself.
 
     precision 'mixed': FP32 Krylov corrections inside FP64 iterative refinement whose
     residual v_f - K_ff lam_f is the matrix-free FP64 tangent action; it stops at the
@@ -330,10 +335,20 @@ def adjoint_solve(problem, dofs, v, adjoint_solver_options=None, precision="fp64
     b = v.clone()
     if eng.n_bc:
         b[eng.bc_rows_long] = 0.0
+    symmetric = eng.tangent_symmetric
     if spec.custom is not None:
         A = eng.tangent(dofs, _lib.FEM_F64, _lib.FEM_BC_SYMMETRIC)
+        A = A if symmetric else A.transpose()
         return torch.as_tensor(spec.custom(A, b, None, spec.options), dtype=torch.float64, device=dofs.device)
     t0 = time.perf_counter()
+    if not symmetric:
+        At = eng.tangent(dofs, _lib.FEM_F64, _lib.FEM_BC_SYMMETRIC).transpose()
+        lam = torch.zeros_like(b)
+        _, _, st = eng.krylov(spec.method, At, b, lam, spec.pc, spec.rtol, spec.atol, spec.maxiter)
+        if st == _lib.FEM_SOLVE_NAN:
+            raise FloatingPointError("adjoint solve produced NaN")
+        _timed(eng, "linear", t0)
+        return lam
     if prec_opt == "fp64":
         A = eng.tangent(dofs, _FP64_SOLVER_FORMAT, _lib.FEM_BC_SYMMETRIC)
         lam = torch.zeros_like(b)
@@ -368,6 +383,21 @@ def adjoint_solve(problem, dofs, v, adjoint_solver_options=None, precision="fp64
             break
     _timed(eng, "linear", t0)
     return lam
+
+
+def dirichlet_adjoint(problem, dofs, v, lam):
+    """lam_b = v_b - K_fb^T lam_f: the Dirichlet rows of A^T lam = v (solver.py:1405-1409) with
+    A = [[K_ff, K_fb], [0, I]] (zeroRows).  K^T lam_f is the FP64 tangent action for a symmetric
+    tangent and the transposed FP64 CSR tangent otherwise.  Returns lam_b in bc_rows order."""
+    eng = problem._engine
+    rows = eng.bc_rows_long
+    lam_f = lam.clone()
+    lam_f[rows] = 0.0
+    if eng.tangent_symmetric:
+        kt = eng.apply(dofs, lam_f, skip_bc_rows=False)
+    else:
+        kt = eng.tangent(dofs, _lib.FEM_F64, _lib.FEM_BC_NONE, cache=False).transpose().matvec(lam_f)
+    return v[rows] - kt[rows]
 
 
 def _iv_cotangent(iv, g, eng, what):
@@ -417,9 +447,18 @@ def implicit_vjp(problem, sol_list, params, v_list, adjoint_solver_options, prec
             if torch.is_tensor(iv) and iv.requires_grad:
                 ivs.append(iv)
                 gos.append(_iv_cotangent(iv, cot[what], eng, what).to(iv.dtype))
+        eng.refresh_bc()
+        if eng.bc_value_terms:
+            # Dirichlet values built from params (set_params -> update_Dirichlet_boundary_conditions):
+            # c_b = u_b - g(p), so -lam^T dc/dp gets +lam_b^T dg/dp
+            with torch.no_grad():
+                lam_b = dirichlet_adjoint(problem, dofs, v, lam)
+            for pos, t in eng.bc_value_terms:
+                ivs.append(t)
+                gos.append(lam_b[pos].to(t.device, t.dtype))
         if not ivs:
-            raise RuntimeError("set_params must build internal_vars from params with torch operations so the "
-                               "parameter chain rule can be applied")
+            raise RuntimeError("set_params must build internal_vars (or Dirichlet values) from params with torch "
+                               "operations so the parameter chain rule can be applied")
         diff_ps = [p for p in ps if torch.is_tensor(p) and p.requires_grad]
         gs = torch.autograd.grad(ivs, diff_ps, grad_outputs=gos, allow_unused=True)
     with torch.no_grad():

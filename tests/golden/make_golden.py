@@ -1,8 +1,8 @@
 """Extract the reference's own FEniCSx gold fixtures into small compressed npz files.
 
-Run here (where the reference tree is mounted) with
+Run, where a checkout of the reference (deepmodeling/jax-fem) is available, with
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path to the reference checkout>
 
 It reads the ASCII VTU files and .npy arrays that the reference's regression
 tests compare against (tests/benchmarks/*/fenicsx/) and writes
@@ -67,4 +67,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path to the reference checkout>")
+    main(sys.argv[1])

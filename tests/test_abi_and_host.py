@@ -227,6 +227,26 @@ def test_surface_map_split_probe():
         P._surface_map_split(lambda u, xx: np.array([u[0] * u[1], 0.0, 0.0]), x, 3)
 
 
+def test_map_probes_see_local_u_dependence():
+    """A mass or surface map that depends on u only on part of the domain (here x < 0.5) must be
+    refused, not integrated as a constant load: the probes check every quadrature point.  Maps
+    written with per-point branching (not vectorisable) and vectorised ones are both covered."""
+    import importlib
+    P = importlib.import_module("jax_fem_gb300.problem")
+    x = np.random.default_rng(1).uniform(0, 1, (400, 3))
+    loc_branch = lambda u, xx: np.array([0.0, 0.0, 1.0]) + (u if xx[0] < 0.5 else 0.0 * u)
+    loc_vector = lambda u, xx: np.array([0.0 * u[0], 0.0 * u[1], 1.0 + 0.0 * u[2]]) + u * (xx[0] < 0.5)
+    for fn in (loc_branch, loc_vector):
+        with pytest.raises(NotImplementedError):
+            P._u_independent(fn, x, 3, "mass map")
+    # u only on half of the faces, linear there: not x-independent, so refused as a Robin map too
+    with pytest.raises(NotImplementedError):
+        P._surface_map_split(loc_branch, x, 3)
+    # genuinely u-independent maps still pass and return their values at every point
+    val = P._u_independent(lambda u, xx: np.array([xx[0], 0.0, -1.0]), x, 3, "mass map").reshape(-1, 3)
+    assert np.allclose(val[:, 0], x[:, 0]) and np.allclose(val[:, 2], -1.0)
+
+
 @pytest.mark.parametrize("binary", [True, False])
 def test_save_sol_vtu_round_trip(tmp_path, binary):
     """save_sol (utils.py:13-57) writes a VTU whose points, cells, 'sol' (float32) and cell /

@@ -284,6 +284,26 @@ def test_mixed_precision_matches_fp64(cuda, mode):
     assert np.abs(gmx - g64).max() <= 1e-8 * np.abs(g64).max()
 
 
+def test_mixed_refine_delta_large_converges(cuda):
+    """refine_delta = 0.9: each reliable update then cuts the squared true residual by only about
+    0.81, which must count as progress (no FEM_SOLVE_STAGNATED on a converging solve); forward and
+    adjoint solves converge and match FP64 like the default delta."""
+    import cases
+    prob, _, theta_np = cases.simp_box(12, 6, 3)
+    o64 = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}, "rel_tol": 1e-12, "tol": 0.0}
+    a64 = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}}
+    s64, J64, g64 = _simp_grad(prob, theta_np, cuda, o64, a64)
+    eng = prob._engine
+    eng.solve_log.clear()
+    smx, Jmx, gmx = _simp_grad(prob, theta_np, cuda, dict(o64, precision="mixed", refine_delta=0.9),
+                               dict(a64, precision="mixed", refine_delta=0.9))
+    refined = [r for r in eng.solve_log if r["method"] == "cg-refined"]
+    assert len(refined) >= 2 and all(r["status"] == "converged" for r in refined), refined
+    assert all(r["updates"] > 5 for r in refined)   # delta 0.9: many small replacements
+    assert (smx - s64).abs().max().item() <= 1e-9 * s64.abs().max().item()
+    assert np.abs(gmx - g64).max() <= 1e-8 * np.abs(g64).max()
+
+
 @pytest.mark.parametrize("n", [(1, 1, 1), (3, 1, 1), (4, 2, 1), (3, 3, 3), (5, 3, 2)])
 def test_small_and_ragged_meshes(cuda, n):
     """Meshes of 8, 16, 30, 64 and 72 nodes: below one 32-node tile (the update kernels' partial
