@@ -29,6 +29,10 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# The CPU port runs its SpMV on a thread pool of its own; BLAS level-1 calls between the SpMVs
+# run single-threaded, or idle BLAS worker threads spin against that pool (measured: 2.5x slower
+# PCG iterations).  Set before numpy loads its BLAS.
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
 
 import numpy as np  # noqa: E402
 
@@ -167,13 +171,14 @@ def spmv_roofline(prob, peak):
     out = {}
     n, nnz, nnzb = eng.num_dofs, eng.nnz, eng.nnzb
     L_ = jf._lib
-    fmts = ((L_.FEM_SYM_DF48, "sym_df48", 6, 8, 16), (L_.FEM_SLICED_DF48, "df48", 6, 8, 8),
+    fmts = ((L_.FEM_SSYM_DF48, "ssym_df48", 6, 8, 16), (L_.FEM_SYM_DF48, "sym_df48", 6, 8, 16),
+            (L_.FEM_SLICED_DF48, "df48", 6, 8, 8),
             (L_.FEM_SLICED_F32, "fp32", 4, 4, 4), (L_.FEM_SLICED_F64, "fp64", 8, 8, 8))
     for prec, name, es, xs, ys in fmts:
         A = eng._tangent_cache.get((prec, jf._lib.FEM_BC_SYMMETRIC))
         if A is None:
             continue
-        if prec in (L_.FEM_SLICED_DF48, L_.FEM_SYM_DF48):
+        if prec in (L_.FEM_SLICED_DF48, L_.FEM_SYM_DF48, L_.FEM_SSYM_DF48):
             pad = 4 if eng.vec == 3 else 1
             x = torch.zeros(eng.num_nodes, pad, 2, dtype=torch.float32, device="cuda")
             x[:, :eng.vec, 0] = torch.randn(eng.num_nodes, eng.vec, device="cuda")
@@ -205,7 +210,13 @@ def spmv_roofline(prob, peak):
         ev[1].record(s)
         torch.cuda.synchronize()
         t = ev[0].elapsed_time(ev[1]) / 1e3 / reps
-        if prec == L_.FEM_SYM_DF48:
+        if prec == L_.FEM_SSYM_DF48:
+            # the 14 stored stencil blocks of every grid row (zero blocks at the boundary included,
+            # implicit columns); x read, y (double-float) and the FP64 transposed part written once
+            gx, gy, gz = eng.grid
+            rows_stored = ((gx * gy + 31) // 32) * 32 * gz
+            algo = rows_stored * 14 * 9 * es + n * xs + n * ys
+        elif prec == L_.FEM_SYM_DF48:
             # the upper node blocks only; y is the double-float direct part plus the FP64
             # transposed part (atomics), both written once per dof
             nb_u = (nnzb - eng.num_nodes) // 2 + eng.num_nodes
@@ -245,73 +256,167 @@ def traffic_from_profile(n_units, kind="df48"):
     return None
 
 
-def cpu_baseline(n, iters_full, seconds_budget=20.0):
-    """Time the oracle (numpy/scipy FP64) on a bounded sample and scale to the full workload."""
-    import torch
-    from oracle import fem as ofem, simp_fast
-    sample = (80, 40, 20)
-    pts, cells = ofem.box_mesh(*sample, *L)
-    N = 3 * len(pts)
-    left = np.isclose(pts[:, 0], 0.0, atol=1e-5)
-    bc_rows = (3 * np.argwhere(left).reshape(-1)[:, None] + np.arange(3)[None, :]).reshape(-1)
-    # surface load on x = Lx: f = sum over face quad points of t N_a nanson (t = (0,0,1))
-    op = ofem.OracleProblem(pts, cells, 3, location_fns=[lambda p: np.isclose(p[0], L[0], atol=1e-5)],
-                            tensor_map=None, surface_maps=[lambda u, x: torch.tensor([0.0, 0.0, 1.0])])
-    f = op.compute_residual(torch.zeros(N)).numpy()
-    th = theta_init(len(cells)).numpy()
-    t0 = time.perf_counter()
-    sc = simp_fast.SimpCantilever(pts, cells, bc_rows, f)
-    t_setup = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    A = sc.assemble(th)
-    t_asm = time.perf_counter() - t0
-    k = 600
-    threads = len(os.sched_getaffinity(0))
-    t0 = time.perf_counter()
-    sc.pcg(A, sc.f, 1e-30, iters=k, threads=threads)
-    t_pcg = (time.perf_counter() - t0) / k
-    t0 = time.perf_counter()
-    u, _ = sc.pcg(A, sc.f, 1e-30, iters=5, threads=threads)
-    dE = 3.0 * (1 - 1e-3) * th.reshape(-1) ** 2
-    _ = -dE * np.einsum("ci,cij,cj->c", u[sc.dofs], sc.K0, u[sc.dofs])
-    t_vjp = time.perf_counter() - t0 - 5 * t_pcg
-    _, cells_full, nodes_full, nnz_full = workload_name(n)
-    cs = len(cells)
-    nnz_s = A.nnz
-    est = (t_setup + t_asm) * cells_full / cs + t_pcg * nnz_full / nnz_s * (iters_full[0] + iters_full[1]) + \
-        max(t_vjp, 0.0) * cells_full / cs
+class CpuPort:
+    """The oracle port of one SIMP TO iteration (oracle/simp_fast.py: FP64 numpy/scipy) built at the
+    workload's own size on the host: element stiffnesses, the COO -> CSR slot map of the PETSc
+    pattern, the end-face load.  Each cost is then timed on the full-size objects: one assembly
+    (E(theta) K0_e summed into the CSR slots, Dirichlet elimination, block-Jacobi set-up), block-
+    Jacobi PCG iterations (SpMV on row blocks in a thread pool over the host cores, vector work
+    numpy), the residual SpMV and the parameter VJP."""
+
+    def __init__(self, n, threads):
+        from oracle import fem as ofem, simp_fast
+        t0 = time.perf_counter()
+        pts, cells = ofem.box_mesh(*n, *L)
+        left = np.isclose(pts[:, 0], 0.0, atol=1e-5)
+        right = np.isclose(pts[:, 0], L[0], atol=1e-5)
+        bc_rows = (3 * np.argwhere(left).reshape(-1)[:, None] + np.arange(3)[None, :]).reshape(-1)
+        f = simp_fast.traction_load(pts, cells, right, [0.0, 0.0, 1.0])
+        self.sc = simp_fast.SimpCantilever(pts, cells, bc_rows, f)
+        _ = self.sc.csr_map
+        self.simp_fast = simp_fast
+        self.theta = theta_init(len(cells)).numpy()
+        self.threads = threads
+        self.cells = len(cells)
+        self.setup_s = time.perf_counter() - t0
+        self.A = self.At = self.P = None
+
+    def assemble(self):
+        t0 = time.perf_counter()
+        self.A = self.sc.assemble_csr(self.theta)
+        self.P = self.sc.csr_map.block_jacobi(self.A)
+        t = time.perf_counter() - t0
+        self.At = self.simp_fast.ThreadedCSR(self.A, self.threads)
+        return t
+
+    def spmv(self, reps=3):
+        x = np.random.default_rng(0).standard_normal(self.sc.N)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            self.At @ x
+        return (time.perf_counter() - t0) / reps
+
+    def pcg_iteration(self, iters):
+        t0 = time.perf_counter()
+        self.sc.pcg(self.At, self.sc.f, 1e-30, iters=iters, precond=self.P)
+        return (time.perf_counter() - t0) / iters
+
+    def solve(self, rtol):
+        t0 = time.perf_counter()
+        u, it = self.sc.pcg(self.At, self.sc.f, rtol, precond=self.P)
+        return u, it, time.perf_counter() - t0
+
+    def vjp(self, u):
+        t0 = time.perf_counter()
+        th = self.theta.reshape(-1)
+        dE = 3.0 * (1 - 1e-3) * th ** 2
+        ue = u[self.sc.dofs]
+        g = -dE * np.einsum("ci,cij,cj->c", ue, self.sc.K0, ue)
+        return g, time.perf_counter() - t0
+
+
+def _blas_threads():
     try:
         from threadpoolctl import threadpool_info
-        blas = max((i.get("num_threads", 1) for i in threadpool_info()), default=1)
+        return max((i.get("num_threads", 1) for i in threadpool_info() if i.get("user_api") == "blas"), default=1)
     except Exception:  # noqa: BLE001
-        blas = 1
-    return {"value": est, "unit": UNIT, "cores": int(threads), "kind": "port",
-            "sample": (f"oracle (numpy/scipy FP64) on HEX8 {sample[0]}x{sample[1]}x{sample[2]} ({cs} cells): "
-                       f"element tangents + COO assembly {t_setup + t_asm:.2f}s, {k} Jacobi-PCG iterations "
-                       f"{t_pcg * 1e3:.2f} ms each, VJP; scaled by cells and nnz to the full workload with "
-                       f"{iters_full[0]}+{iters_full[1]} PCG iterations (forward+adjoint); SpMV is scipy's "
-                       f"CSR kernel on {threads} row blocks in a thread pool, element tangents and assembly "
-                       f"numpy, BLAS threads {blas}"),
-            "host_cores": len(os.sched_getaffinity(0))}
+        return 1
+
+
+# systems up to this many dofs are solved to the tolerance on the host (nothing projected);
+# larger ones time PCG iterations at full size and take the iteration counts of the GPU's FP64 run
+CPU_SOLVE_DOFS = 400_000
+
+
+def cpu_baseline(n, iters_full, pcg_sample=10, port=None):
+    """One TO iteration of the oracle port on the host cores, every unit cost timed at the
+    workload's full size.  Small workloads run to the tolerance (value_kind 'measured'); at full
+    size the forward and adjoint block-Jacobi PCG iteration counts are those of the GPU's FP64
+    block-Jacobi run (value_kind 'projected': assembly, residual SpMVs and VJP measured once each,
+    PCG iterations timed in a sample of `pcg_sample`)."""
+    threads = len(os.sched_getaffinity(0))
+    port = port or CpuPort(n, threads)
+    t_asm = port.assemble()
+    t_spmv = port.spmv()
+    name, cells, nodes, nnz = workload_name(n)
+    if port.sc.N <= CPU_SOLVE_DOFS:
+        u, it_f, t_f = port.solve(RTOL)
+        _, it_a, t_a = port.solve(RTOL)          # adjoint: A^T lam = dJ/du = f (compliance)
+        _, t_vjp = port.vjp(u)
+        value = t_asm + 2 * t_spmv + t_f + t_a + t_vjp
+        kind = "measured"
+        proj = {"assembly_s": t_asm, "residual_spmv_s": t_spmv, "forward_s": t_f, "adjoint_s": t_a, "vjp_s": t_vjp,
+                "pcg_iterations": [it_f, it_a], "setup_s": port.setup_s}
+        how = (f"forward + adjoint block-Jacobi PCG to {RTOL:g} on the host ({it_f} + {it_a} iterations, "
+               f"{t_f + t_a:.2f} s)")
+    else:
+        t_it = port.pcg_iteration(pcg_sample)
+        # the VJP's cost does not depend on the values of u: time it on a seeded field
+        _, t_vjp = port.vjp(np.random.default_rng(0).standard_normal(port.sc.N))
+        value = t_asm + 2 * t_spmv + t_it * (iters_full[0] + iters_full[1]) + t_vjp
+        kind = "projected"
+        proj = {"assembly_s": t_asm, "residual_spmv_s": t_spmv, "pcg_iteration_s": t_it, "vjp_s": t_vjp,
+                "pcg_iterations": list(iters_full), "pcg_iterations_source": "GPU FP64 block-Jacobi run",
+                "setup_s": port.setup_s}
+        how = (f"{pcg_sample} block-Jacobi PCG iterations timed at full size ({t_it * 1e3:.1f} ms each) x "
+               f"{iters_full[0]}+{iters_full[1]} iterations (forward+adjoint, counts of the GPU FP64 run)")
+    sample = (f"oracle (numpy/scipy FP64) at the full {n[0]}x{n[1]}x{n[2]} size ({cells} cells, {port.sc.N} dofs, "
+              f"nnz {port.sc.csr_map.nnz}): assembly {t_asm:.2f} s (E K0_e summed into the PETSc-pattern CSR "
+              f"slots, Dirichlet elimination, block-Jacobi set-up; numpy, one thread), residual SpMV "
+              f"{t_spmv * 1e3:.1f} ms x 2, {how}, VJP {t_vjp:.2f} s; SpMV is scipy's CSR kernel on "
+              f"{threads} row blocks in a thread pool, vector work BLAS level 1 in place on "
+              f"{_blas_threads()} BLAS thread(s)")
+    out = {"value": value, "unit": UNIT, "cores": int(threads), "kind": "port", "value_kind": kind, "sample": sample,
+           "host_cores": len(os.sched_getaffinity(0)), "components": proj}
+    return out, port
 
 
 def bench_reference(args):
+    """The reference arm: the oracle port of the same iteration on all host cores.  Set-up and
+    the once-per-iteration costs (assembly, residual SpMVs, VJP) are measured once at full size;
+    each step times a sample of block-Jacobi PCG iterations at full size (or, for small
+    workloads, a complete forward + adjoint solve), and the line's value is the iteration
+    assembled from those measured unit costs."""
     n = tuple(args.size)
     name, cells, nodes, nnz = workload_name(n)
     iters = FULL_SIZE_PCG_ITERS if n == DEFAULT_SIZE else _default_iters(n)
-    vals = []
+    threads = len(os.sched_getaffinity(0))
+    port = CpuPort(n, threads)
+    first, port = cpu_baseline(n, iters, port=port)
+    small = port.sc.N <= CPU_SOLVE_DOFS
+    samples = []
     for _ in range(args.warmup):
-        cpu_baseline(n, iters)
+        if small:
+            port.solve(RTOL)
+        else:
+            port.pcg_iteration(10)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        vals.append(cpu_baseline(n, iters))
+        if small:
+            _, _, tf = port.solve(RTOL)
+            samples.append(tf)
+        else:
+            samples.append(port.pcg_iteration(10))
     wall = time.perf_counter() - t0
-    v = statistics.median([x["value"] for x in vals])
-    cb = dict(vals[-1], value=v)
+    comp = first["components"]
+    if small:
+        # both solves are the same system and right-hand side (compliance is self-adjoint)
+        t_solve = statistics.median(samples) if samples else 0.5 * (comp["forward_s"] + comp["adjoint_s"])
+        v = comp["assembly_s"] + 2 * comp["residual_spmv_s"] + 2 * t_solve + comp["vjp_s"]
+    else:
+        t_it = statistics.median(samples) if samples else comp["pcg_iteration_s"]
+        comp["pcg_iteration_s"] = t_it
+        v = comp["assembly_s"] + 2 * comp["residual_spmv_s"] + t_it * sum(iters) + comp["vjp_s"]
+    cb = dict(first, value=v)
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall / max(args.steps, 1) * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": name, "precision": "fp64", "tolerance": RTOL, "solver": "Jacobi PCG (scipy CSR SpMV on all host cores)"},
+            "value_kind": first["value_kind"],
+            "config": {"workload": name, "precision": "fp64", "tolerance": RTOL,
+                       "solver": "block-Jacobi PCG (scipy CSR SpMV on all host cores)",
+                       "step": ("one forward block-Jacobi PCG solve to the tolerance at full size" if small else
+                                "10 block-Jacobi PCG iterations at full size (ms_per_step is this sample's wall "
+                                "time; value is the whole iteration from the measured unit costs)")},
             "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -703,13 +808,14 @@ def main():
     # ---- CPU baseline (rank 0, N=1) ----------------------------------------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        it_full = (its_64[0], its_64[1]) if fp64 is not None and len(its_64) >= 2 else _default_iters(n)
+        it_full = (its_64[0], its_64[1]) if fp64 is not None and len(its_64) >= 2 else \
+            (FULL_SIZE_PCG_ITERS if n == DEFAULT_SIZE else _default_iters(n))
         try:
-            cpu = cpu_baseline(n, it_full)
+            cpu, _ = cpu_baseline(n, it_full)
         except Exception as exc:  # noqa: BLE001
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
 
-    head = "sym_df48" if "sym_df48" in roof else "df48"
+    head = "ssym_df48" if "ssym_df48" in roof else "sym_df48" if "sym_df48" in roof else "df48"
     f32 = roof.get(head, roof.get("fp32", {}))
     isolated = dict(f32)
     if spmv_in_loop.get("launches_timed") and f32.get("algorithmic_bytes"):
@@ -735,7 +841,11 @@ def main():
         "e2e": {"value": t_e2e / args.steps / world, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": f32.get("achieved_gbs"), "peak": peak, "unit": "GB/s",
                      "frac": f32.get("frac"), "traffic": traffic,
-                     "kernel": ("spmv_sliced_dfdf_bulk_kernel<3,SYM> (fem_spmv_dfx: FEM_SYM_DF48 upper node blocks, "
+                     "kernel": ("spmv_ssym_bulk_kernel (fem_spmv_dfx: FEM_SSYM_DF48 structured symmetric stencil "
+                                "storage, implicit columns, transposed half in registers / warp shuffles, plane i+1 by "
+                                "FP64 atomics; bulk-copy staged, double-float on FP32 pipes; timed call includes the "
+                                "FP64 zero-fill and fold of the transposed part)" if head == "ssym_df48" else
+                                "spmv_sliced_dfdf_bulk_kernel<3,SYM> (fem_spmv_dfx: FEM_SYM_DF48 upper node blocks, "
                                 "transposed half by FP64 atomics, bulk-copy staged, double-float on FP32 pipes; "
                                 "timed call includes the FP64 zero-fill and fold of the transposed half)"
                                 if head == "sym_df48" else

@@ -63,7 +63,15 @@ enum {
    * slice_cols_u; padding slots point at the row itself with zero values).  The SpMV adds
    * A_ij x_j to row i and A_ij^T x_i to row j (FP64 atomics into a separate FP64 vector),
    * so it reads about half the bytes; its result is not bitwise reproducible. */
-  FEM_SYM_DF48 = 6
+  FEM_SYM_DF48 = 6,
+  /* Structured symmetric DF48 (vec 3): for a node grid numbered node = (i*ny + j)*nz + k
+   * (fem_pattern_t.grid_nx/ny/nz set), the diagonal and the 13 upper neighbours of the 27-point
+   * stencil per node row with implicit columns, value v of slot s of row (line L, k) at
+   * (((L/32)*nz + k)*14 + s)*288 + v*32 + L%32 (hi floats, then the int16 corrections at
+   * round_up(4*m, 256); 256 bytes more hold the converter's pattern check).  The SpMV keeps the
+   * transposed half in registers and warp shuffles and sends the rest (plane i+1 and the warp
+   * edges) to an FP64 vector by atomics, so its result is not bitwise reproducible. */
+  FEM_SSYM_DF48 = 7
 };
 enum {                                                       /* built-in tensor maps     */
   FEM_MAT_LAPLACE = 1,        /* consts: [k]                      test_linear_poisson.py:15-17 */
@@ -75,7 +83,8 @@ enum {                                                       /* built-in tensor 
   FEM_MAT_J2 = 6              /* consts: [E, nu, sig0]; history sigma_old|eps_old (18/qp);
                                  optional qp param s scaling E      test_plasticity.py:32-78 */
 };
-enum { FEM_OUT_RESIDUAL = 1, FEM_OUT_MATRIX = 2, FEM_OUT_APPLY = 4 };
+enum { FEM_OUT_RESIDUAL = 1, FEM_OUT_MATRIX = 2, FEM_OUT_APPLY = 4,
+       FEM_OUT_PARAM_VJP = 8 /* run-time compiled kernels only: -lam^T dR/d(internal vars) */ };
 enum {
   FEM_BC_NONE = 0,
   FEM_BC_ROWS = 1,      /* skip Dirichlet rows (PETSc zeroRows semantics, solver.py:527-528) */
@@ -111,6 +120,8 @@ typedef struct fem_pattern_t {
   int64_t n_slots_u;        /* upper-block sliced layout (fem_pattern_slices_upper)  */
   const int64_t* slice_ptr_u;
   const int32_t* slice_cols_u;/* padding: the row's own node                         */
+  int64_t grid_nx, grid_ny, grid_nz; /* node grid of a structured box numbering          */
+                            /* node = (i*ny + j)*nz + k, or 0 when not structured   */
 } fem_pattern_t;
 
 typedef struct fem_material_t {
@@ -121,6 +132,37 @@ typedef struct fem_material_t {
   const double* qp_params;  /* (n_cells, nq, n_qp_params) or NULL                 */
   const double* history;    /* J2: (n_cells, nq, 18) = sigma_old(9) | eps_old(9)  */
 } fem_material_t;
+
+/* Parameter block of the run-time compiled (user) kernels, fem_jit_launch.  Every field is 8 bytes
+ * wide so the generated kernel's copy of the struct has the same layout.
+ *   coords/conn: the mesh; n_items: cells (cell kernel) or faces (face kernel);
+ *   face_cells/face_ids: the faces' cell and local face (face kernels);
+ *   u: dofs; w: direction of FEM_OUT_APPLY; lam: multiplier of FEM_OUT_PARAM_VJP;
+ *   iv: per-cell internal variables, iv_stride doubles per cell (per face for face kernels);
+ *   indptr/slots: CSR rows and per-cell slot table (FEM_OUT_MATRIX); bc/bc_mode: Dirichlet mask
+ *   and handling as fem_assemble; outputs: FEM_OUT_* bits;
+ *   res/vals/apply_out: atomically accumulated FP64 outputs; vjp_out: iv_stride values per item. */
+typedef struct fem_jit_params_t {
+  const double* coords;
+  const int32_t* conn;
+  int64_t n_items;
+  const int32_t* face_cells;
+  const int32_t* face_ids;
+  const double* u;
+  const double* w;
+  const double* lam;
+  const double* iv;
+  int64_t iv_stride;
+  const int64_t* indptr;
+  const uint8_t* slots;
+  const uint8_t* bc;
+  int64_t bc_mode;
+  int64_t outputs;
+  double* res;
+  double* vals;
+  double* apply_out;
+  double* vjp_out;
+} fem_jit_params_t;
 
 /* ---- library ------------------------------------------------------------- */
 const char* fem_last_error(void);
@@ -389,6 +431,18 @@ int fem_dr_measure(int64_t n, double h, double h_tilde, const double* R, const d
  * qdd = (qdot - qdot_old)/h (solver.py:1020-1022). */
 int fem_dr_velocity(int64_t n, double h, double c, const double* R, const double* M, double* qdot, double* qdot_old,
                     double* qdd, double* qdd_old, void* stream);
+
+/* ---- run-time compiled user kernels ---------------------------------------
+ * The reference compiles the user's weak-form functions with XLA (jax.jit(jax.vmap(kernel)),
+ * problem.py:335-338, including get_universal_kernel at :289-294 and
+ * get_universal_kernels_surface at :318-323).  Here the Python layer traces such a function
+ * into CUDA C++ and these two calls compile and run it.
+ * fem_jit_load: compile `source` with NVRTC for the current device and load it (cached per
+ *   source and device); *module receives an opaque handle.  FEM_ERR_ARG carries the compiler log.
+ * fem_jit_launch: run the generated kernel `kernel` over n_items cells or faces with the
+ *   parameter block P (copied at call time) on `stream`. */
+int fem_jit_load(const char* source, void** module);
+int fem_jit_launch(void* module, const char* kernel, const fem_jit_params_t* params, int64_t n_items, void* stream);
 
 #ifdef __cplusplus
 }

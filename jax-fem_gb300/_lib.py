@@ -12,10 +12,10 @@ LIB_PATH = os.path.join(HERE, "libjaxfem_gb300.so")
 # ---- constants mirrored from the header --------------------------------------
 FEM_OK, FEM_ERR_ARG, FEM_ERR_CUDA, FEM_ERR_UNSUPPORTED, FEM_ERR_CAPACITY, FEM_ERR_DEVICE = range(6)
 FEM_HEX8, FEM_TET10, FEM_TET4 = 1, 2, 3
-FEM_F32, FEM_F64, FEM_DF48, FEM_SLICED_F32, FEM_SLICED_F64, FEM_SLICED_DF48, FEM_SYM_DF48 = range(7)
+FEM_F32, FEM_F64, FEM_DF48, FEM_SLICED_F32, FEM_SLICED_F64, FEM_SLICED_DF48, FEM_SYM_DF48, FEM_SSYM_DF48 = range(8)
 (FEM_MAT_LAPLACE, FEM_MAT_LINEAR_ELASTIC, FEM_MAT_SIMP, FEM_MAT_GENERAL_LINEAR,
  FEM_MAT_NEO_HOOKEAN, FEM_MAT_J2) = range(1, 7)
-FEM_OUT_RESIDUAL, FEM_OUT_MATRIX, FEM_OUT_APPLY = 1, 2, 4
+FEM_OUT_RESIDUAL, FEM_OUT_MATRIX, FEM_OUT_APPLY, FEM_OUT_PARAM_VJP = 1, 2, 4, 8
 FEM_BC_NONE, FEM_BC_ROWS, FEM_BC_SYMMETRIC = 0, 1, 2
 FEM_PC_NONE, FEM_PC_JACOBI, FEM_PC_BJACOBI = 0, 1, 2
 FEM_SOLVE_CONVERGED, FEM_SOLVE_MAXITER, FEM_SOLVE_BREAKDOWN, FEM_SOLVE_NAN, FEM_SOLVE_STAGNATED = range(5)
@@ -42,7 +42,16 @@ class FemPattern(C.Structure):
                 ("indptr", C.c_void_p), ("diag", C.c_void_p), ("slots", C.c_void_p),
                 ("n_slices", C.c_int64), ("n_slots", C.c_int64), ("slice_ptr", C.c_void_p),
                 ("slice_cols", C.c_void_p), ("n_slots_u", C.c_int64), ("slice_ptr_u", C.c_void_p),
-                ("slice_cols_u", C.c_void_p)]
+                ("slice_cols_u", C.c_void_p), ("grid_nx", C.c_int64), ("grid_ny", C.c_int64),
+                ("grid_nz", C.c_int64)]
+
+
+class FemJitParams(C.Structure):
+    _fields_ = [("coords", C.c_void_p), ("conn", C.c_void_p), ("n_items", C.c_int64), ("face_cells", C.c_void_p),
+                ("face_ids", C.c_void_p), ("u", C.c_void_p), ("w", C.c_void_p), ("lam", C.c_void_p),
+                ("iv", C.c_void_p), ("iv_stride", C.c_int64), ("indptr", C.c_void_p), ("slots", C.c_void_p),
+                ("bc", C.c_void_p), ("bc_mode", C.c_int64), ("outputs", C.c_int64), ("res", C.c_void_p),
+                ("vals", C.c_void_p), ("apply_out", C.c_void_p), ("vjp_out", C.c_void_p)]
 
 
 class FemMaterial(C.Structure):
@@ -111,6 +120,8 @@ SIGNATURES = {
     "fem_filter_workspace": ([I64, PSZ], C.c_int),
     "fem_filter_build": ([I64, P, F64, I32, P, P, P, P, SZ, P], C.c_int),
     "fem_filter_apply": ([I64, I32, P, P, P, P, P, I32, I32, P, P], C.c_int),
+    "fem_jit_load": ([C.c_char_p, C.POINTER(C.c_void_p)], C.c_int),
+    "fem_jit_launch": ([P, C.c_char_p, C.POINTER(FemJitParams), I64, P], C.c_int),
 }
 
 _lib = None

@@ -38,7 +38,7 @@ struct KCtl {
 };
 
 static bool is_sliced(int p) { return p == FEM_SLICED_F32 || p == FEM_SLICED_F64 || p == FEM_SLICED_DF48 || p == FEM_SYM_DF48; }
-static bool is_df(int p) { return p == FEM_DF48 || p == FEM_SLICED_DF48 || p == FEM_SYM_DF48; }
+static bool is_df(int p) { return p == FEM_DF48 || p == FEM_SLICED_DF48 || p == FEM_SYM_DF48 || p == FEM_SSYM_DF48; }
 // FP32 vectors for FP32 matrices, FP64 vectors otherwise
 static bool vec_f32(int p) { return p == FEM_F32 || p == FEM_SLICED_F32; }
 
@@ -260,6 +260,30 @@ __device__ __forceinline__ df2 df_of(double d) {
   return df2{h, __double2float_rn(d - (double)h)};
 }
 __device__ __forceinline__ double df_dbl(df2 a) { return (double)a.h + (double)a.l; }
+
+// An FP64 value as a double-float pair built from its bits with integer and FP32 operations only
+// (GB300's FP64 pipe runs ~1/64 of the FP32 rate): h keeps the sign, the exponent and the leading
+// 24 significand bits, l the next 29 bits (rounded to 24), renormalised.  For |v| inside FP32's
+// normal range; the CG's vectors are range-scaled to an RMS near 1.  Values whose l would fall
+// below FP32's normal range keep h only (|v| below ~2^-74: far under the vectors' rounding).
+__device__ __forceinline__ df2 df_from_bits(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+  const int e = (int)((hw >> 20) & 0x7FFu) - 1023;          // unbiased exponent
+  const unsigned sgn = hw & 0x80000000u;
+  if (e < -126) return df2{0.f, 0.f};
+  if (e > 127) return df2{__int_as_float(sgn | 0x7F800000u), 0.f};
+  const float h = __int_as_float(sgn | ((unsigned)(e + 127) << 23) | ((hw & 0xFFFFFu) << 3) | (lw >> 29));
+  float l = 0.f;
+  if (e - 52 >= -126) l = __int_as_float(sgn | 0x3F800000u) * (float)(lw & 0x1FFFFFFFu) *
+                          __int_as_float((unsigned)(e - 52 + 127) << 23);
+  return df_fast(h, l);
+}
+
+// Component stride of the FP64 transposed-part vector qT of the symmetric SpMVs (component c of
+// node i at c * qt_stride + i): the node count rounded up to 32, so that each component of a
+// 32-node tile is one 256-byte run (a bulk copy needs 16-byte aligned runs).
+__host__ __device__ __forceinline__ int64_t qt_stride(int64_t n_nodes) { return (n_nodes + 31) & ~int64_t(31); }
 // accumulate a*b into (sh, sl) without renormalising every step
 __device__ __forceinline__ void df_acc(float& sh, float& sl, df2 a, df2 b) {
   const float p = a.h * b.h;
@@ -815,7 +839,7 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
 #pragma unroll
                   for (int r = 0; r < VEC; ++r)
                     df_acc(th, tl, df2{ah[r * VEC + d], al[r * VEC + d]}, df2{xih[r], xil[r]});
-                  atomicAdd(qT + (int64_t)d * n_nodes + j, (double)th + (double)tl);   // component-major
+                  atomicAdd(qT + (int64_t)d * qt_stride(n_nodes) + j, (double)th + (double)tl);   // component-major
                 }
               }
             }
@@ -872,20 +896,24 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
   reduce_and_finalize_df<1>(dv, C, op, partials, C->ticket, &C->d0);
 }
 
-// y (df) += qT (FP64, component-major: component c of node i at c * n_nodes + i), qT = 0: the
+// y (df) += qT (FP64, component-major: component c of node i at c * qt_stride + i), qT = 0: the
 // FEM_SYM_DF48 SpMV's transposed part folded into its result (vec 3)
 __global__ void sym_combine_kernel(int64_t n_nodes, float* __restrict__ yh, float* __restrict__ yl,
                                    double* __restrict__ qT) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < 3 * n_nodes;
        k += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = k / 3;
-    const int64_t t = (k - 3 * i) * n_nodes + i;
-    const df2 y = df_add(df2{yh[k], yl[k]}, df_of(qT[t]));
+    const int64_t t = (k - 3 * i) * qt_stride(n_nodes) + i;
+    const df2 y = df_add(df2{yh[k], yl[k]}, df_from_bits(qT[t]));
     yh[k] = y.h;
     yl[k] = y.l;
     qT[t] = 0.0;
   }
 }
+
+}  // namespace fem
+#include "fem_ssym.cuh"
+namespace fem {
 
 // FP64 CSR values -> sliced layout (FP64, FP32 or DF48 hi/lo), thread per (slice, lane).
 template <int VEC, int OUT>
@@ -1296,8 +1324,8 @@ pcgx_update_tile_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
         xl[k] = x.l;
         df2 qv{qh[k], ql[k]};
         if constexpr (SYM) {   // q = direct part (df) + transposed part (FP64, component-major), consumed here
-          const int64_t t = (int64_t)c * n_nodes + node0 + nl;
-          qv = df_add(qv, df_of(qT[t]));
+          const int64_t t = (int64_t)c * qt_stride(n_nodes) + node0 + nl;
+          qv = df_add(qv, df_from_bits(qT[t]));
           qT[t] = 0.0;
         }
         const df2 r = df_add(df2{rh[k], rl[k]}, df_mul(na, qv));
@@ -1352,24 +1380,28 @@ pcgx_update_tile_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
 constexpr int UPD_WARPS = 4;
 constexpr int UPD_STAGES = 3;
 
-template <int PC>
+template <int PC, bool SYM = false>
 struct UpdGeom {
   static constexpr int PCW = PC == FEM_PC_BJACOBI ? 9 : PC == FEM_PC_JACOBI ? 3 : 0;
   static constexpr uint32_t VB = 96 * 4;        // one dof-ordered float array of a tile
   static constexpr uint32_t PB = 32 * 4 * 8;    // p: 32 nodes x 4 (hi, lo) pairs
   static constexpr uint32_t CB = 32 * PCW * 4;  // preconditioner blocks
-  static constexpr uint32_t STAGE = 6 * VB + PB + CB;
+  static constexpr uint32_t QB = SYM ? 3 * 32 * 8 : 0;   // SYM: the tile's qT, three component runs
+  static constexpr uint32_t STAGE = 6 * VB + PB + CB + QB;
   static constexpr uint32_t BAR_BYTES = 128;    // UPD_WARPS * UPD_STAGES barriers, padded
   static constexpr uint32_t SMEM = BAR_BYTES + UPD_WARPS * UPD_STAGES * STAGE;
 };
 
-template <int PC>
+// SYM: q is the double-float part of A p plus the FP64 transposed part qT of a symmetric SpMV
+// (component c of node i at c * qt_stride + i), streamed with the tile and zeroed once consumed.
+template <int PC, bool SYM = false>
 __global__ void __launch_bounds__(UPD_WARPS * 32)
 pcgx_update_bulk_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restrict__ xl, float* __restrict__ rh,
                         float* __restrict__ rl, float* __restrict__ z, const float2* __restrict__ pp,
                         const float* __restrict__ qh, const float* __restrict__ ql, const float* __restrict__ pc,
-                        KCtl* C, double* partials, int op) {
-  using G = UpdGeom<PC>;
+                        KCtl* C, double* partials, int op, double* __restrict__ qT = nullptr) {
+  using G = UpdGeom<PC, SYM>;
+  const int64_t qs = qt_stride(n_nodes);
   constexpr int PCW = G::PCW;
   extern __shared__ __align__(128) unsigned char smem[];
   if (C->done) return;
@@ -1406,6 +1438,10 @@ pcgx_update_bulk_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
       bulk_load(st + 5 * G::VB, ql + d0, G::VB, bar);
       bulk_load(st + 6 * G::VB, pp + pt * 128, G::PB, bar);
       if constexpr (PCW > 0) bulk_load(st + 6 * G::VB + G::PB, pc + pt * 32 * PCW, G::CB, bar);
+      if constexpr (SYM) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) bulk_load(st + 6 * G::VB + G::PB + G::CB + c * 256, qT + c * qs + pt * 32, 256, bar);
+      }
     }
     pt += nw;
     return true;
@@ -1421,6 +1457,7 @@ pcgx_update_bulk_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
     const float* sql = sxh + 480;
     const float2* spp = reinterpret_cast<const float2*>(st + 6 * G::VB);
     const float* spc = reinterpret_cast<const float*>(st + 6 * G::VB + G::PB);
+    const double* sqt = reinterpret_cast<const double*>(st + 6 * G::VB + G::PB + G::CB);
     const int nd = 3 * nn;
     const int64_t d0 = t * 96;
 #pragma unroll
@@ -1432,7 +1469,9 @@ pcgx_update_bulk_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
         const df2 x = df_add(df2{sxh[o], sxl[o]}, df_mul(a, df2{pv.x, pv.y}));
         xh[d0 + o] = x.h;
         xl[d0 + o] = x.l;
-        const df2 r = df_add(df2{srh[o], srl[o]}, df_mul(na, df2{sqh[o], sql[o]}));
+        df2 qv{sqh[o], sql[o]};
+        if constexpr (SYM) qv = df_add(qv, df_from_bits(sqt[c * 32 + nl]));
+        const df2 r = df_add(df2{srh[o], srl[o]}, df_mul(na, qv));
         rh[d0 + o] = r.h;
         rl[d0 + o] = r.l;
         srh[o] = r.h;
@@ -1467,6 +1506,11 @@ pcgx_update_bulk_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
     for (int j = 0; j < 3; ++j) {
       const int o = 32 * j + lane;
       if (o < nd) z[d0 + o] = sqh[o];
+    }
+    if constexpr (SYM) {   // the transposed part is consumed: zero it for the next SpMV
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        if (lane < nn) qT[c * qs + t * 32 + lane] = 0.0;
     }
     async_proxy_fence();   // this lane's shared-memory writes before the stage's next bulk copy
     __syncwarp();
@@ -1516,6 +1560,10 @@ pcgx_update_bulk_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
     if constexpr (PCW > 0) {
       float* spc = reinterpret_cast<float*>(ring + 6 * G::VB + G::PB);
       for (int o = lane; o < 32 * PCW; o += 32) spc[o] = o < PCW * nn ? pc[nfull * 32 * PCW + o] : 0.f;
+    }
+    if constexpr (SYM) {
+      double* sqt = reinterpret_cast<double*>(ring + 6 * G::VB + G::PB + G::CB);
+      for (int c = 0; c < 3; ++c) sqt[c * 32 + lane] = lane < nn ? qT[c * qs + nfull * 32 + lane] : 0.0;
     }
     __syncwarp();
     compute(ring, nfull, nn);
@@ -1942,15 +1990,15 @@ static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 // The mixed CG's update (vec 3, general storage) by the bulk-copy staged kernel; false when an
 // array is not 16-byte aligned (the caller then launches pcgx_update_tile_kernel).  Grid:
 // resident CTAs, capped by the tiles.
-template <int PC>
+template <int PC, bool SYM = false>
 static bool launch_update_bulk(int64_t n_nodes, float* xh, float* xl, float* rh, float* rl, float* z,
                                const float2* pp, const float* qh, const float* ql, const float* pc, KCtl* C,
-                               double* partials, int op, cudaStream_t s) {
-  using G = UpdGeom<PC>;
+                               double* partials, int op, cudaStream_t s, double* qT = nullptr) {
+  using G = UpdGeom<PC, SYM>;
   if (!(aligned16(xh) && aligned16(xl) && aligned16(rh) && aligned16(rl) && aligned16(pp) && aligned16(qh) &&
-        aligned16(ql) && (G::PCW == 0 || aligned16(pc))))
+        aligned16(ql) && (G::PCW == 0 || aligned16(pc)) && (!SYM || aligned16(qT))))
     return false;
-  auto kern = pcgx_update_bulk_kernel<PC>;
+  auto kern = pcgx_update_bulk_kernel<PC, SYM>;
   constexpr int smem = (int)G::SMEM;
   static int per_sm = 0;
   if (per_sm == 0) {
@@ -1965,7 +2013,7 @@ static bool launch_update_bulk(int64_t n_nodes, float* xh, float* xl, float* rh,
   if (g > need) g = need;
   if (g > MAX_PARTIAL_BLOCKS) g = MAX_PARTIAL_BLOCKS;
   if (g < 1) g = 1;
-  kern<<<(unsigned)g, UPD_WARPS * 32, smem, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C, partials, op);
+  kern<<<(unsigned)g, UPD_WARPS * 32, smem, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C, partials, op, qT);
   return true;
 }
 
@@ -2008,6 +2056,43 @@ static int launch_dfdf(const fem_pattern_t* pat, int64_t n_nodes, const float* v
     if (g < 1) g = 1;
     kern<<<(unsigned)g, SPMV_THREADS, 0, s>>>(n_nodes, ns, sp, sc, vhi, vlo, xp, yh, yl, C, op, partials);
   }
+  note_launches(1);
+  return FEM_OK;
+}
+
+// The structured symmetric SpMV (FEM_SSYM_DF48).  Work items are (group of 32 lines, k range);
+// the number of k ranges per group is chosen so that the items fill the resident warps with the
+// fewest rounds of the longest item (a partly filled last round costs a whole item's time).
+// Grid: min(items, resident warps) warps.  Needs 16-byte aligned values and corrections.
+static int launch_ssym(const fem_pattern_t* pat, const float* vhi, const int16_t* vlo, const float2* xp, float* yh,
+                       float* yl, double* qT, KCtl* C, int op, double* partials, cudaStream_t s) {
+  if (!(aligned16(vhi) && aligned16(vlo) && qT))
+    return fail(FEM_ERR_ARG, "FEM_SSYM_DF48 needs 16-byte aligned values and a transposed-part vector");
+  auto kern = spmv_ssym_bulk_kernel;
+  constexpr int smem = (int)SsGeom::SMEM;
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, SS_WARPS * 32, smem) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+  }
+  const int64_t resident = (int64_t)sm_count() * per_sm * SS_WARPS;
+  const SsGrid G0 = ss_grid(pat, 1);
+  int best = 1;
+  int64_t best_cost = INT64_MAX;
+  for (int c = 1; c <= (int)std::min<int64_t>(G0.nz, 64); ++c) {
+    const int64_t rounds = (G0.groups * c + resident - 1) / resident;
+    const int64_t cost = rounds * ((G0.nz + c - 1) / c);
+    if (cost < best_cost) { best_cost = cost; best = c; }
+  }
+  const SsGrid G = ss_grid(pat, best);
+  int64_t warps = std::min<int64_t>(G.groups * G.chunks, resident);
+  int64_t g = (warps + SS_WARPS - 1) / SS_WARPS;
+  if (g > MAX_PARTIAL_BLOCKS) g = MAX_PARTIAL_BLOCKS;
+  if (g < 1) g = 1;
+  kern<<<(unsigned)g, SS_WARPS * 32, smem, s>>>(G, vhi, vlo, xp, yh, yl, qT, C, op, partials);
   note_launches(1);
   return FEM_OK;
 }
@@ -2254,6 +2339,7 @@ static inline size_t df_lo_offset(int64_t nnz) { return al(sizeof(float) * (size
 // Number of stored values of a matrix in `mfmt` (sliced layouts include their padding).
 static inline int64_t n_values(const fem_pattern_t* pat, int vec, int mfmt) {
   if (mfmt == FEM_SYM_DF48) return pat->n_slots_u * vec * vec * 32;
+  if (mfmt == FEM_SSYM_DF48) return ((pat->grid_nx * pat->grid_ny + 31) / 32) * pat->grid_nz * SS_SLOTS * 9 * 32;
   if (mfmt >= FEM_SLICED_F32) return pat->n_slots * vec * vec * 32;
   return pat->nnzb * vec * vec;
 }
@@ -2266,13 +2352,18 @@ static inline int64_t n_values(const fem_pattern_t* pat, int vec, int mfmt) {
 // as float pairs (FP32 pipes only); the FP64 true residual b - K x (matrix-free tangent
 // action) replaces r whenever the recursive residual has fallen by `delta`, and is the
 // only convergence test.  x (FP64, caller's buffer) is read at start and written back.
-template <int VEC, int PC, bool SYM = false>
+// MODE: DFX_SLICED (FEM_SLICED_DF48), DFX_SYM (FEM_SYM_DF48), DFX_SSYM (FEM_SSYM_DF48).  The two
+// symmetric storages leave part of A p in the FP64 vector qT, which the update kernel folds in.
+enum { DFX_SLICED = 0, DFX_SYM = 1, DFX_SSYM = 2 };
+template <int VEC, int PC, int MODE = DFX_SLICED>
 static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* vals, const float* pc, const RefOp& op,
                         const double* b, double* x, double rtol, double atol, double delta, int64_t maxiter,
                         void* ws, int64_t* iters, int64_t* updates, double* rnorm, int32_t* status, cudaStream_t s) {
+  constexpr bool SYM = MODE != DFX_SLICED;
   const uint8_t* bc = op.bc;
   const int64_t n = n_nodes * VEC;
-  const int64_t m = n_values(pat, VEC, SYM ? FEM_SYM_DF48 : FEM_SLICED_DF48);
+  const int64_t m = n_values(pat, VEC, MODE == DFX_SSYM ? FEM_SSYM_DF48 : MODE == DFX_SYM ? FEM_SYM_DF48
+                                                                                          : FEM_SLICED_DF48);
   const float* vhi = static_cast<const float*>(vals);
   const int16_t* vlo = reinterpret_cast<const int16_t*>(static_cast<const char*>(vals) + df_lo_offset(m));
   KWs w = carve(ws, n, FEM_F64);
@@ -2289,7 +2380,7 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
   double* ax = reinterpret_cast<double*>(v); v += d8;
   double* r64 = reinterpret_cast<double*>(v); v += d8;
   double* qT = SYM ? reinterpret_cast<double*>(v) : nullptr;   // transposed part of the SYM SpMV
-  if (SYM) FEM_CUDA(cudaMemsetAsync(qT, 0, sizeof(double) * (size_t)n, s));
+  if (SYM) FEM_CUDA(cudaMemsetAsync(qT, 0, sizeof(double) * (size_t)(VEC * qt_stride(n_nodes)), s));
   KCtl* C = w.ctl;
   const int gv = vec_grid(n), gn = vec_grid(n_nodes);
   // tile kernel: one warp per 32-node tile, grid = resident CTAs (no partial second wave)
@@ -2384,12 +2475,15 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
       }
       for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
         if (k == 0) spmv_timer_mark(0, s);
-        rc = launch_dfdf<VEC, SYM>(pat, n_nodes, vhi, vlo, pp, qh, ql, C, FIN_PCG_ALPHA, w.partials, s, qT);
+        if constexpr (MODE == DFX_SSYM)
+          rc = launch_ssym(pat, vhi, vlo, pp, qh, ql, qT, C, FIN_PCG_ALPHA, w.partials, s);
+        else
+          rc = launch_dfdf<VEC, SYM>(pat, n_nodes, vhi, vlo, pp, qh, ql, C, FIN_PCG_ALPHA, w.partials, s, qT);
         if (rc) return rc;
         if (k == 0) spmv_timer_mark(1, s);
         if constexpr (VEC == 3) {
-          if (SYM || !launch_update_bulk<PC>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C, w.partials,
-                                             FIN_PCGR_UPDATE, s))
+          if (!launch_update_bulk<PC, SYM>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C, w.partials,
+                                           FIN_PCGR_UPDATE, s, qT))
             pcgx_update_tile_kernel<PC, SYM><<<gt, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
                                                                      w.partials, FIN_PCGR_UPDATE, qT);
           pcgx_direction3_kernel<<<gv, VTHREADS, 0, s>>>(n, z, pp, C);
@@ -2513,7 +2607,11 @@ static int check_pat(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int
   FEM_REQUIRE(pat && pat->block_ptr && pat->block_cols, "pattern NULL");
   FEM_REQUIRE(n_nodes > 0, "n_nodes must be positive");
   FEM_REQUIRE(vec == 1 || vec == 3, "vec must be 1 or 3");
-  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SYM_DF48, "bad precision");
+  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SSYM_DF48, "bad precision");
+  FEM_REQUIRE(precision != FEM_SSYM_DF48 ||
+                  (vec == 3 && pat->grid_nx > 0 && pat->grid_ny > 0 && pat->grid_nz > 0 &&
+                   pat->grid_nx * pat->grid_ny * pat->grid_nz == n_nodes),
+              "FEM_SSYM_DF48 needs vec 3 and the pattern's node grid (grid_nx*grid_ny*grid_nz == n_nodes)");
   FEM_REQUIRE(!is_sliced(precision) || (pat->n_slices == (n_nodes + 31) / 32 && pat->slice_ptr && pat->slice_cols),
               "sliced format needs the pattern's slice arrays (fem_pattern_slices)");
   FEM_REQUIRE(precision != FEM_SYM_DF48 || (pat->slice_ptr_u && pat->slice_cols_u && pat->n_slots_u > 0),
@@ -2525,7 +2623,8 @@ extern "C" int fem_spmv(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, 
                         const void* x, void* y, void* stream) {
   int rc = check_pat(pat, n_nodes, vec, precision);
   if (rc) return rc;
-  FEM_REQUIRE(precision != FEM_SYM_DF48, "FEM_SYM_DF48 matrices are applied by fem_spmv_dfx");
+  FEM_REQUIRE(precision != FEM_SYM_DF48 && precision != FEM_SSYM_DF48,
+              "FEM_SYM_DF48 / FEM_SSYM_DF48 matrices are applied by fem_spmv_dfx");
   FEM_REQUIRE(vals && x && y, "NULL vector");
   cudaStream_t s = as_stream(stream);
   if (is_df(precision)) {
@@ -2627,7 +2726,7 @@ extern "C" int fem_precond_setup(const fem_pattern_t* pat, int64_t n_nodes, int3
 
 extern "C" int fem_krylov_workspace(int64_t n_dofs, int32_t precision, size_t* bytes) {
   FEM_REQUIRE(bytes && n_dofs >= 0, "bad arguments");
-  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SYM_DF48, "bad precision");
+  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SSYM_DF48, "bad precision");
   *bytes = krylov_ws_bytes(n_dofs, vec_f32(precision) ? FEM_F32 : FEM_F64);
   return FEM_OK;
 }
@@ -2782,9 +2881,12 @@ extern "C" int fem_pcg_refined(const fem_pattern_t* pat, int64_t n_nodes, int32_
   const float* P = (const float*)pc32;
 #define FEM_REF_CASE(VEC, PC)                                                                                   \
   if (vec == VEC && pc_kind == PC)                                                                              \
-    return precision == FEM_SYM_DF48                                                                            \
-               ? pcg_dfx_impl<VEC, PC, true>(pat, n_nodes, vals32, P, op, b, x, rtol, atol, delta, maxiter, ws, \
-                                             iterations, updates, res_norm, status, s)                         \
+    return precision == FEM_SSYM_DF48                                                                           \
+               ? pcg_dfx_impl<VEC, PC, DFX_SSYM>(pat, n_nodes, vals32, P, op, b, x, rtol, atol, delta, maxiter, \
+                                                 ws, iterations, updates, res_norm, status, s)                 \
+           : precision == FEM_SYM_DF48                                                                          \
+               ? pcg_dfx_impl<VEC, PC, DFX_SYM>(pat, n_nodes, vals32, P, op, b, x, rtol, atol, delta, maxiter,  \
+                                                ws, iterations, updates, res_norm, status, s)                  \
            : precision == FEM_SLICED_DF48                                                                       \
                ? pcg_dfx_impl<VEC, PC>(pat, n_nodes, vals32, P, op, b, x, rtol, atol, delta, maxiter, ws,       \
                                        iterations, updates, res_norm, status, s)                               \
@@ -2805,11 +2907,14 @@ extern "C" int fem_pcg_refined(const fem_pattern_t* pat, int64_t n_nodes, int32_
 
 extern "C" int fem_matrix_bytes(const fem_pattern_t* pat, int32_t vec, int32_t precision, size_t* bytes) {
   FEM_REQUIRE(pat && bytes && (vec == 1 || vec == 3), "bad arguments");
-  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SYM_DF48, "bad precision");
+  FEM_REQUIRE(precision >= FEM_F32 && precision <= FEM_SSYM_DF48, "bad precision");
   FEM_REQUIRE(!is_sliced(precision) || pat->n_slices > 0, "sliced format needs fem_pattern_slices first");
   FEM_REQUIRE(precision != FEM_SYM_DF48 || pat->n_slots_u > 0, "FEM_SYM_DF48 needs fem_pattern_slices_upper first");
+  FEM_REQUIRE(precision != FEM_SSYM_DF48 || (vec == 3 && pat->grid_nx > 0 && pat->grid_ny > 0 && pat->grid_nz > 0),
+              "FEM_SSYM_DF48 needs vec 3 and the pattern's node grid");
   const int64_t m = n_values(pat, vec, precision);
-  if (is_df(precision)) *bytes = df_lo_offset(m) + sizeof(int16_t) * (size_t)m;
+  if (precision == FEM_SSYM_DF48) *bytes = al(df_lo_offset(m) + sizeof(int16_t) * (size_t)m) + 256;
+  else if (is_df(precision)) *bytes = df_lo_offset(m) + sizeof(int16_t) * (size_t)m;
   else if (vec_f32(precision)) *bytes = sizeof(float) * (size_t)m;
   else *bytes = sizeof(double) * (size_t)m;
   return FEM_OK;
@@ -2823,7 +2928,23 @@ extern "C" int fem_matrix_convert(const fem_pattern_t* pat, int64_t n_nodes, int
   FEM_REQUIRE(precision != FEM_F64, "FP64 CSR values need no conversion");
   cudaStream_t s = as_stream(stream);
   const int64_t nnz = pat->nnzb * vec * vec;
-  if (precision == FEM_SYM_DF48) {
+  if (precision == FEM_SSYM_DF48) {
+    const int64_t m = n_values(pat, vec, precision);
+    int16_t* lo = reinterpret_cast<int16_t*>((char*)out + df_lo_offset(m));
+    int* err = reinterpret_cast<int*>((char*)out + al(df_lo_offset(m) + sizeof(int16_t) * (size_t)m));
+    FEM_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    const SsGrid G = ss_grid(pat, 1);
+    to_ssym_kernel<<<grid_for(G.groups * G.nz * 32, 256), 256, 0, s>>>(G, pat->block_ptr, pat->block_cols, vals64,
+                                                                        (float*)out, lo, err);
+    note_launches(1);
+    int rc2 = check_launch("matrix_convert (ssym)");
+    if (rc2) return rc2;
+    int h = 0;
+    FEM_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FEM_CUDA(cudaStreamSynchronize(s));
+    if (h) return fail(FEM_ERR_ARG, "FEM_SSYM_DF48: the node pattern is not the 27-point stencil of the grid");
+    return FEM_OK;
+  } else if (precision == FEM_SYM_DF48) {
     FEM_REQUIRE(vec == 3, "FEM_SYM_DF48 is built for vec 3");
     const int64_t m = n_values(pat, vec, precision);
     int16_t* lo = reinterpret_cast<int16_t*>((char*)out + df_lo_offset(m));
@@ -2869,7 +2990,8 @@ extern "C" int fem_spmv_dfx(const fem_pattern_t* pat, int64_t n_nodes, int32_t v
                             const void* vals, const void* x_df, float* y_hi, float* y_lo, double* xy_dot, void* ws,
                             size_t ws_bytes, void* stream) {
   FEM_REQUIRE(pat && vals && x_df && y_hi && y_lo && ws, "NULL argument");
-  FEM_REQUIRE(precision == FEM_SLICED_DF48 || precision == FEM_SYM_DF48, "precision must be a sliced DF48 type");
+  FEM_REQUIRE(precision == FEM_SLICED_DF48 || precision == FEM_SYM_DF48 || precision == FEM_SSYM_DF48,
+              "precision must be a sliced or symmetric DF48 type");
   int rc0 = check_pat(pat, n_nodes, vec, precision);
   if (rc0) return rc0;
   FEM_REQUIRE(ws_bytes >= krylov_ws_bytes(n_nodes * vec, FEM_F64), "workspace too small");
@@ -2882,10 +3004,13 @@ extern "C" int fem_spmv_dfx(const fem_pattern_t* pat, int64_t n_nodes, int32_t v
   note_launches(1);
   const float2* xp = static_cast<const float2*>(x_df);
   int rc;
-  if (precision == FEM_SYM_DF48) {
+  if (precision == FEM_SYM_DF48 || precision == FEM_SSYM_DF48) {
     double* qT = reinterpret_cast<double*>(w.vecs);
-    FEM_CUDA(cudaMemsetAsync(qT, 0, sizeof(double) * (size_t)(n_nodes * vec), s));
-    rc = launch_dfdf<3, true>(pat, n_nodes, vhi, vlo, xp, y_hi, y_lo, w.ctl, FIN_DOT, w.partials, s, qT);
+    FEM_CUDA(cudaMemsetAsync(qT, 0, sizeof(double) * (size_t)(vec * qt_stride(n_nodes)), s));
+    if (precision == FEM_SSYM_DF48)
+      rc = launch_ssym(pat, vhi, vlo, xp, y_hi, y_lo, qT, w.ctl, FIN_DOT, w.partials, s);
+    else
+      rc = launch_dfdf<3, true>(pat, n_nodes, vhi, vlo, xp, y_hi, y_lo, w.ctl, FIN_DOT, w.partials, s, qT);
     if (rc) return rc;
     sym_combine_kernel<<<vec_grid(n_nodes * vec), VTHREADS, 0, s>>>(n_nodes, y_hi, y_lo, qT);
     note_launches(1);

@@ -17,6 +17,36 @@ from ._lib import call, ptr
 from .logger import logger
 
 
+def structured_grid(points, rtol=1e-9):
+    """(nx, ny, nz) node counts when node n sits at grid point (i, j, k) of a tensor-product grid
+    with n = (i*ny + j)*nz + k -- x slowest, z fastest, the numbering of box_mesh
+    (jax_fem/generate_mesh.py:151-189) -- else None.  Coordinates are compared to the grid lines
+    within rtol of the box size; the converter to the structured storage then checks every node
+    row's pattern against the grid's stencil."""
+    P = np.asarray(points, dtype=np.float64)
+    N = len(P)
+    if N < 2 or P.shape[1] != 3:
+        return None
+    tol = rtol * max(float(np.ptp(P, axis=0).max()), 1e-300)
+    moved_xy = np.nonzero((np.abs(P[:, 0] - P[0, 0]) > tol) | (np.abs(P[:, 1] - P[0, 1]) > tol))[0]
+    nz = int(moved_xy[0]) if len(moved_xy) else N
+    moved_x = np.nonzero(np.abs(P[:, 0] - P[0, 0]) > tol)[0]
+    nyz = int(moved_x[0]) if len(moved_x) else N
+    if nz < 1 or nyz % nz or N % nyz:
+        return None
+    ny, nx = nyz // nz, N // nyz
+    G = P.reshape(nx, ny, nz, 3)
+    if not (np.all(np.abs(G[:, :, :, 0] - G[:, :1, :1, 0]) <= tol) and
+            np.all(np.abs(G[:, :, :, 1] - G[:1, :, :1, 1]) <= tol) and
+            np.all(np.abs(G[:, :, :, 2] - G[:1, :1, :, 2]) <= tol)):
+        return None
+    for ax, n in ((0, nx), (1, ny), (2, nz)):
+        line = G[:, 0, 0, 0] if ax == 0 else G[0, :, 0, 1] if ax == 1 else G[0, 0, :, 2]
+        if n > 1 and not np.all(np.diff(line) > tol):
+            return None
+    return nx, ny, nz
+
+
 def _stream():
     return _lib.stream_handle()
 
@@ -50,7 +80,7 @@ class DeviceCSR:
         return self.eng.scalar_indices()
 
     def matvec(self, x):
-        if self.precision == _lib.FEM_SYM_DF48:
+        if self.precision in (_lib.FEM_SYM_DF48, _lib.FEM_SSYM_DF48):
             return self._matvec_dfx(x)
         if self.precision in (_lib.FEM_DF48, _lib.FEM_SLICED_DF48):
             x = x.to(torch.float64).contiguous()
@@ -184,6 +214,8 @@ class Engine:
         self.f_ext = torch.zeros(self.num_dofs, dtype=torch.float64, device=dev)
         self._loads_done = False
         self._robin = []            # (face_cells, face_ids, degree, coeffs) of u-dependent surface maps
+        self._uk = None             # compiled universal kernels (get_universal_kernel[s_surface])
+        self._uk_key = None
 
     def add_robin(self, boundary_inds, coeffs):
         """Register the u-dependent polynomial part of a surface map on the faces boundary_inds."""
@@ -247,11 +279,16 @@ class Engine:
         self.slice_cols_u = torch.empty(self.n_slots_u * 32, dtype=torch.int32, device=dev)
         call("fem_pattern_slices_upper", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols),
              ptr(self.slice_ptr_u), ptr(self.slice_cols_u), None, s)
+        # node grid of a structured box numbering (the FEM_SSYM_DF48 solver copy), vec 3 and
+        # elements whose nodes couple only grid neighbours
+        self.grid = structured_grid(self.fe.points) if self.vec == 3 and self.fe.ele_type in ("HEX8", "TET4") \
+            else None
+        gx, gy, gz = self.grid if self.grid is not None else (0, 0, 0)
         self.pattern = _lib.FemPattern(self.nnzb, self.block_ptr.data_ptr(), self.block_cols.data_ptr(),
                                        self.indptr.data_ptr(), self.diag.data_ptr(), self.slots.data_ptr(),
                                        self.n_slices, self.n_slots, self.slice_ptr.data_ptr(),
                                        self.slice_cols.data_ptr(), self.n_slots_u, self.slice_ptr_u.data_ptr(),
-                                       self.slice_cols_u.data_ptr())
+                                       self.slice_cols_u.data_ptr(), gx, gy, gz)
         self._indices = None
 
     def scalar_indices(self):
@@ -311,7 +348,7 @@ class Engine:
     def tangent_symmetric(self):
         """Whether K(u) is symmetric: the material's tangent (Robin parts are symmetric)."""
         m, _ = self.material()
-        return bool(m.symmetric)
+        return bool(m.symmetric) and not self.has_universal   # a compiled user kernel may be non-symmetric
 
     # ---- external loads (mass / surface maps independent of u) -----------------------
     def refresh_loads(self):
@@ -385,6 +422,8 @@ class Engine:
              _lib.FEM_F64, ptr(dofs), None, None, _lib.FEM_BC_NONE, ptr(res), None, None, _stream())
         if self._robin:
             self._robin_call(_lib.FEM_OUT_RESIDUAL, _lib.FEM_F64, dofs, res=res)
+        if self.has_universal:
+            self._universal_call(_lib.FEM_OUT_RESIDUAL, dofs, res=res)
         if apply_bc:
             self.refresh_bc()
             if self.n_bc:
@@ -397,8 +436,10 @@ class Engine:
         FEM_DF48 matrices are assembled in FP64 and split into the 6-byte double-float format."""
         self.refresh_bc()
         m, ms = self.material()
+        if precision == _lib.FEM_SSYM_DF48 and (self.grid is None or bc_mode != _lib.FEM_BC_SYMMETRIC):
+            precision = _lib.FEM_SLICED_DF48      # no structured copy for this mesh / elimination
         key = (precision, bc_mode)
-        if cache and m.linear and self.robin_linear and key in self._tangent_cache:
+        if cache and m.linear and self.robin_linear and not self.has_universal and key in self._tangent_cache:
             return self._tangent_cache[key]
         if precision not in (_lib.FEM_F32, _lib.FEM_F64):
             # solver copies (DF48, sliced FP32 / FP64 / DF48) are converted from the FP64 CSR tangent
@@ -410,8 +451,18 @@ class Engine:
             if buf is None or buf.numel() != nb.value:
                 buf = torch.empty(nb.value, dtype=torch.uint8, device=self.device)
                 setattr(self, name, buf)
-            call("fem_matrix_convert", C.byref(self.pattern), self.num_nodes, self.vec, ptr(A64.data), precision,
-                 ptr(buf), _stream())
+            try:
+                call("fem_matrix_convert", C.byref(self.pattern), self.num_nodes, self.vec, ptr(A64.data), precision,
+                     ptr(buf), _stream())
+            except _lib.FemError as exc:
+                if precision != _lib.FEM_SSYM_DF48:
+                    raise
+                # the node pattern is not the grid's stencil (the converter checked every row):
+                # no structured copy for this mesh, the general sliced layout instead
+                logger.info("structured symmetric storage refused (%s); sliced DF48 instead", exc)
+                self.grid = None
+                self.pattern.grid_nx = self.pattern.grid_ny = self.pattern.grid_nz = 0
+                return self.tangent(dofs, _lib.FEM_SLICED_DF48, bc_mode, cache=cache)
             view = buf.view(torch.float64) if precision == _lib.FEM_SLICED_F64 else \
                 buf.view(torch.float32) if precision == _lib.FEM_SLICED_F32 else buf
             A = DeviceCSR(self, precision, view, bc_mode, source=A64)
@@ -429,6 +480,12 @@ class Engine:
              precision, ptr(dofs), None, ptr(self.bc_mask), bc_mode, None, ptr(vals), None, _stream())
         if self._robin:
             self._robin_call(_lib.FEM_OUT_MATRIX, precision, dofs, bc_mode=bc_mode, bc=self.bc_mask, vals=vals)
+        if self.has_universal:
+            if precision != _lib.FEM_F64:
+                raise NotImplementedError("universal kernels assemble FP64 tangents (the solver copies are "
+                                          "converted from them)")
+            self._universal_call(_lib.FEM_OUT_MATRIX, dofs, bc=self.bc_mask if bc_mode != _lib.FEM_BC_NONE else None,
+                                 bc_mode=bc_mode, vals=vals)
         if bc_mode != _lib.FEM_BC_NONE and self.n_bc:
             call("fem_zero_rows", C.byref(self.pattern), self.vec, precision, ptr(vals), ptr(self.bc_rows), self.n_bc,
                  1.0, _stream())
@@ -447,7 +504,107 @@ class Engine:
         if self._robin:
             self._robin_call(_lib.FEM_OUT_APPLY, _lib.FEM_F64, dofs.contiguous(), w=w.contiguous(),
                              bc=self.bc_mask if skip_bc_rows else None, apply_out=out)
+        if self.has_universal:
+            self._universal_call(_lib.FEM_OUT_APPLY, dofs.contiguous(), w=w.contiguous(),
+                                 bc=self.bc_mask if skip_bc_rows else None, apply_out=out)
         return out
+
+    # ---- compiled universal kernels (get_universal_kernel / get_universal_kernels_surface) ----
+    @property
+    def has_universal(self):
+        p = self.problem
+        return hasattr(p, "get_universal_kernel") or hasattr(p, "get_universal_kernels_surface")
+
+    def _universal_ivs(self):
+        """The internal variables as the universal cell kernel sees them: per cell (nq, ...) arrays,
+        concatenated per cell into one FP64 buffer (num_cells, iv_stride)."""
+        p = self.problem
+        ivs = [torch.as_tensor(t, dtype=torch.float64, device=self.device) for t in p.internal_vars]
+        for t in ivs:
+            if t.dim() < 1 or t.shape[0] != self.num_cells:
+                raise ValueError(f"internal variable of shape {tuple(t.shape)}: the universal kernel needs "
+                                 f"(num_cells, num_quads, ...) arrays")
+        shapes = tuple(tuple(t.shape[1:]) for t in ivs)
+        buf = torch.cat([t.reshape(self.num_cells, -1) for t in ivs], dim=1).contiguous() if ivs else None
+        return ivs, shapes, buf
+
+    def universal(self):
+        """Compiled kernels of the problem's universal kernels, traced again whenever the shapes of
+        the internal variables change."""
+        from . import jit
+        p = self.problem
+        _, shapes, _ = self._universal_ivs()
+        key = shapes
+        if self._uk is not None and self._uk_key == key:
+            return self._uk
+        fe = self.fe
+        t = {k: getattr(fe, k) for k in ("shape_vals", "shape_grads_ref", "quad_weights", "face_shape_vals",
+                                         "face_shape_grads_ref", "face_quad_weights", "face_normals")}
+        cell = face = None
+        if hasattr(p, "get_universal_kernel"):
+            fn_src, ivs = jit.trace_cell(p.get_universal_kernel(), self.nn, self.num_quads, self.vec, shapes)
+            cell = (jit.CompiledKernels(jit.cell_source(fn_src, t, self.nn, self.num_quads, self.vec, ivs), ivs, 0),
+                    ivs)
+        if hasattr(p, "get_universal_kernels_surface"):
+            kernels = p.get_universal_kernels_surface()
+            if len(kernels) != len(p.boundary_inds_list):
+                raise AssertionError("get_universal_kernels_surface must give one kernel per location_fns entry")
+            if any(len(v) for v in p.internal_vars_surfaces):
+                raise NotImplementedError("internal_vars_surfaces are not passed to compiled surface kernels")
+            srcs = [jit.trace_face(fn, self.nn, fe.num_face_quads, self.vec, k) for k, fn in enumerate(kernels)]
+            faces = []
+            for bi in p.boundary_inds_list:
+                bi = np.asarray(bi)
+                faces.append((torch.as_tensor(bi[:, 0].astype(np.int32), device=self.device),
+                              torch.as_tensor(bi[:, 1].astype(np.int32), device=self.device)) if len(bi) else None)
+            face = (jit.CompiledKernels(jit.face_source(srcs, t, self.nn, self.vec, 0), 0, len(srcs)), faces)
+        self._uk, self._uk_key = (cell, face), key
+        return self._uk
+
+    def _universal_call(self, outputs, dofs, w=None, lam=None, bc=None, bc_mode=_lib.FEM_BC_NONE, res=None,
+                        vals=None, apply_out=None, vjp_out=None):
+        from . import jit
+        (cell, face) = self.universal()
+        s = _stream()
+        common = dict(coords=self.coords.data_ptr(), conn=self.conn.data_ptr(), u=dofs.data_ptr(),
+                      w=None if w is None else w.data_ptr(), lam=None if lam is None else lam.data_ptr(),
+                      indptr=self.indptr.data_ptr(), slots=self.slots.data_ptr(),
+                      bc=None if bc is None else bc.data_ptr(), bc_mode=bc_mode, outputs=outputs,
+                      res=None if res is None else res.data_ptr(), vals=None if vals is None else vals.data_ptr(),
+                      apply_out=None if apply_out is None else apply_out.data_ptr())
+        if cell is not None:
+            ck, ivs = cell
+            _, _, buf = self._universal_ivs()
+            self._uk_ivbuf = buf      # alive until the stream has used it
+            P = jit.params(n_items=self.num_cells, iv=None if buf is None else buf.data_ptr(), iv_stride=ivs,
+                           vjp_out=None if vjp_out is None else vjp_out.data_ptr(), **common)
+            ck.launch("fem_ucell", P, self.num_cells, s)
+        if face is not None and not (outputs & _lib.FEM_OUT_PARAM_VJP):
+            fk, faces = face
+            for k, fc in enumerate(faces):
+                if fc is None:
+                    continue
+                P = jit.params(n_items=fc[0].numel(), face_cells=fc[0].data_ptr(), face_ids=fc[1].data_ptr(),
+                               iv=None, iv_stride=0, vjp_out=None, **common)
+                fk.launch(f"fem_uface_{k}", P, fc[0].numel(), s)
+
+    def universal_param_vjp(self, dofs, lam):
+        """-lam^T dR_universal/d(internal vars): a list shaped like problem.internal_vars (lam masked
+        to 0 on Dirichlet dofs), or None without a universal cell kernel."""
+        (cell, _) = self.universal()
+        if cell is None or cell[1] == 0:
+            return None
+        self.refresh_bc()
+        ivs, shapes, _ = self._universal_ivs()
+        out = torch.empty(self.num_cells, cell[1], dtype=torch.float64, device=self.device)
+        self._universal_call(_lib.FEM_OUT_PARAM_VJP, dofs.contiguous(), lam=lam.contiguous(), bc=self.bc_mask,
+                             vjp_out=out)
+        res, o = [], 0
+        for t, sh in zip(ivs, shapes):
+            k = int(np.prod(sh))
+            res.append(out[:, o:o + k].reshape(t.shape))
+            o += k
+        return res
 
     def param_vjp(self, dofs, lam):
         """-lam^T dR/dp per quadrature point (lam masked to 0 on Dirichlet dofs)."""
@@ -525,7 +682,9 @@ class Engine:
              float(rtol), float(atol), float(delta), int(maxiter), ptr(ws), ws.numel(), C.byref(it), C.byref(up),
              C.byref(rn), C.byref(st), _stream())
         rec = dict(method="cg-refined",
-                   precision="df48+fp64" if A32.precision in (_lib.FEM_DF48, _lib.FEM_SLICED_DF48) else "fp32+fp64",
+                   precision={_lib.FEM_DF48: "df48+fp64", _lib.FEM_SLICED_DF48: "df48+fp64",
+                              _lib.FEM_SYM_DF48: "sym-df48+fp64",
+                              _lib.FEM_SSYM_DF48: "ssym-df48+fp64"}.get(A32.precision, "fp32+fp64"),
                    iterations=it.value, updates=up.value,
                    res_norm=rn.value, status=_lib.SOLVE_STATUS.get(st.value, "?"), seconds=time.perf_counter() - t0)
         self.solve_log.append(rec)

@@ -83,14 +83,14 @@ class Problem:
     def _prepare_maps(self):
         fe = self.fes[0]
         eng = self._engine
-        if hasattr(self, "get_universal_kernel") or hasattr(self, "get_universal_kernels_surface"):
-            raise NotImplementedError("universal kernels (user per-cell kernels) are not part of this build")
         n_surf = len(self.boundary_inds_list)
         if hasattr(self, "get_surface_maps"):
             maps = self.get_surface_maps()
             assert n_surf == len(maps)          # problem.py:340-346
         else:
-            assert n_surf == 0, "Missing definitions for surface integral"
+            # surface terms may come from get_universal_kernels_surface alone (problem.py:305-332)
+            assert n_surf == 0 or hasattr(self, "get_universal_kernels_surface"), \
+                "Missing definitions for surface integral"
             maps = []
         if hasattr(self, "get_mass_map"):
             xq, _ = eng.quad_points()
@@ -111,8 +111,18 @@ class Problem:
 
     def _resolve_material(self):
         if not hasattr(self, "get_tensor_map"):
-            raise NotImplementedError("get_tensor_map() is required (laplace kernel, problem.py:283-287)")
+            if hasattr(self, "get_universal_kernel") or hasattr(self, "get_universal_kernels_surface"):
+                # the physics is all in the universal kernels (problem.py:283-294 add no laplace term)
+                return probe_tensor_map(lambda u_grad: 0.0 * u_grad, self.fes[0].vec)
+            raise NotImplementedError("get_tensor_map() or get_universal_kernel() is required "
+                                      "(problem.py:283-294)")
         return probe_tensor_map(self.get_tensor_map(), self.fes[0].vec)
+
+    # ---- helpers the reference's universal kernels call (problem.py:86-92) -------------------
+    def unflatten_fn_dof(self, dof_flat):
+        """Cell dofs (num_nodes*vec,) -> [(num_nodes, vec)] (one variable)."""
+        fe = self.fes[0]
+        return [dof_flat.reshape(fe.num_nodes, fe.vec)]
 
     # ---- reference entry points ------------------------------------------------------
     def unflatten_fn_sol_list(self, dofs):

@@ -7,7 +7,10 @@ Mirrors jax_fem/solver.py (Newton branch, 63-553 and 1079-1455):
     block naming jax_solver / petsc_solver / spsolve_solver / custom_solver.
     Additional keys: 'precision' ('fp64' default; 'mixed': CG on a DF48 copy of
     the FP64 tangent with double-float vectors and FP64 reliable updates;
-    'mixed_sym': the same on upper-block storage; 'mixed32': FP32 matrix and
+    on a structured box grid of HEX8/TET4 nodes 'mixed' stores only the diagonal
+    and upper stencil blocks (FEM_SSYM_DF48); 'mixed_sliced' keeps the general
+    sliced DF48 copy there too; 'mixed_sym': upper-block storage of a general
+    pattern with the transposed half by FP64 atomics; 'mixed32': FP32 matrix and
     vectors with FP64 reliable updates -- BiCGStab under a mixed precision runs
     in FP32 and Newton's FP64 residual refines it), 'inner_rtol' (that
     BiCGStab's tolerance), 'refine_delta', 'max_iter' (Newton cap).
@@ -105,20 +108,25 @@ def resolve_linear(linear_options):
 
 def _precision(cfg):
     p = cfg.get("precision", "fp64")
-    if p not in ("fp64", "mixed", "mixed_sym", "mixed32"):
-        raise ValueError("precision must be 'fp64', 'mixed' (DF48 matrix, double-float vectors), 'mixed_sym' (the same "
+    if p not in ("fp64", "mixed", "mixed_sliced", "mixed_sym", "mixed32"):
+        raise ValueError("precision must be 'fp64', 'mixed' (DF48 matrix, double-float vectors), 'mixed_sliced' "
+                         "(the same, general sliced storage on every mesh), 'mixed_sym' (the same "
                          "with upper-block DF48 storage) or 'mixed32' (FP32)")
     return p
 
 
 def _mixed_matrix_precision(precision, eng=None):
-    """Solver copy of the tangent: sliced DF48 for 'mixed'; the symmetric DF48 layout (upper node
-    blocks, transposed half through FP64 atomics) for 'mixed_sym' when the tangent is symmetric
-    and vec = 3 -- it reads about half the matrix bytes but is slower on GB300 (the FP64 atomics
-    cost more than the bytes saved); sliced FP32 for 'mixed32'."""
+    """Solver copy of the tangent.  'mixed': the structured symmetric DF48 layout (diagonal and
+    upper stencil blocks, implicit columns; the transposed half in registers and warp shuffles)
+    when the nodes form a box grid (eng.grid) and the tangent is symmetric, sliced DF48 otherwise;
+    'mixed_sliced': sliced DF48 always; 'mixed_sym': upper node blocks of the general pattern with
+    the transposed half through FP64 atomics (slower on GB300: the atomics cost more than the
+    bytes saved); sliced FP32 for 'mixed32'."""
     if precision == "mixed_sym" and eng is not None and eng.vec == 3 and getattr(eng._mat, "symmetric", False):
         return _lib.FEM_SYM_DF48
-    if precision in ("mixed", "mixed_sym"):
+    if precision == "mixed" and eng is not None and eng.grid is not None and eng.tangent_symmetric:
+        return _lib.FEM_SSYM_DF48
+    if precision in ("mixed", "mixed_sym", "mixed_sliced"):
         return _lib.FEM_SLICED_DF48
     return _lib.FEM_SLICED_F32
 
@@ -142,7 +150,7 @@ def linear_solver(A, b, x0, linear_options, precision="fp64", inner_rtol=1e-5):
     eng = A.eng
     if spec.custom is not None:
         return spec.custom(A, b, x0, linear_options)
-    if A.precision in (_lib.FEM_DF48, _lib.FEM_SLICED_DF48):
+    if A.precision in (_lib.FEM_DF48, _lib.FEM_SLICED_DF48, _lib.FEM_SYM_DF48, _lib.FEM_SSYM_DF48):
         raise NotImplementedError("DF48 matrices are solved by the mixed Newton / adjoint paths (fem_pcg_refined)")
     x = torch.zeros_like(b) if x0 is None else x0.clone()
     if A.vector_dtype == torch.float64:
@@ -164,7 +172,7 @@ def _newton_step(problem, eng, dofs, res, spec, precision, cfg):
     """One Newton correction A inc = -res (solver.py:390-421) with the Dirichlet rows of the
     increment equal to g - u_b."""
     prec = _FP64_SOLVER_FORMAT if precision == "fp64" else _mixed_matrix_precision(precision, eng)
-    if prec in (_lib.FEM_SLICED_DF48, _lib.FEM_SYM_DF48) and spec.method != "cg":
+    if prec in (_lib.FEM_SLICED_DF48, _lib.FEM_SYM_DF48, _lib.FEM_SSYM_DF48) and spec.method != "cg":
         prec = _lib.FEM_SLICED_F32   # BiCGStab mixed path runs in FP32 with Newton-level refinement
     eng.refresh_bc()
     rows = eng.bc_rows_long
@@ -447,6 +455,15 @@ def implicit_vjp(problem, sol_list, params, v_list, adjoint_solver_options, prec
             if torch.is_tensor(iv) and iv.requires_grad:
                 ivs.append(iv)
                 gos.append(_iv_cotangent(iv, cot[what], eng, what).to(iv.dtype))
+        if eng.has_universal:
+            # the compiled universal kernels' part of -lam^T dR/d(internal vars)
+            with torch.no_grad():
+                ucot = eng.universal_param_vjp(dofs, lam)
+            if ucot is not None:
+                for iv, g in zip(problem.internal_vars, ucot):
+                    if torch.is_tensor(iv) and iv.requires_grad:
+                        ivs.append(iv)
+                        gos.append(g.to(iv.dtype).reshape(iv.shape))
         eng.refresh_bc()
         if eng.bc_value_terms:
             # Dirichlet values built from params (set_params -> update_Dirichlet_boundary_conditions):

@@ -132,10 +132,15 @@ class OracleProblem:
 
     tensor_map(u_grad, *iv_q) -> (vec, dim); mass_map(u, x, *iv_q) -> (vec,);
     surface_maps[i](u, x, *iv_surf) -> (vec,).  All torch, one point at a time.
+    universal_kernel(cell_sol_flat, x, cell_shape_grads, cell_JxW, cell_v_grads_JxW, *iv_cell) and
+    universal_kernels_surface[i](cell_sol_flat, x, face_shape_vals, face_shape_grads, face_nanson_scale)
+    as in problem.py:289-294 and :318-323 (cell_JxW (num_vars, nq), cell_v_grads_JxW (nq, nn, 1, dim),
+    face_nanson_scale (num_vars, nfq)), torch, one cell / face at a time.
     """
 
     def __init__(self, points, cells, vec, ele_type="HEX8", quadrature_order=None, dirichlet_bc_info=None,
-                 location_fns=None, tensor_map=None, mass_map=None, surface_maps=None):
+                 location_fns=None, tensor_map=None, mass_map=None, surface_maps=None, universal_kernel=None,
+                 universal_kernels_surface=None):
         self.fe = OracleFE(points, cells, vec, ele_type, quadrature_order, dirichlet_bc_info)
         self.fes = [self.fe]
         self.vec = vec
@@ -145,8 +150,10 @@ class OracleProblem:
         self.tensor_map = tensor_map
         self.mass_map = mass_map
         self.surface_maps = surface_maps or []
+        self.universal_kernel = universal_kernel
+        self.universal_kernels_surface = universal_kernels_surface or []
         self.boundary_inds_list = self.fe.get_boundary_conditions_inds(location_fns)
-        if len(self.boundary_inds_list) and not self.surface_maps:
+        if len(self.boundary_inds_list) and not (self.surface_maps or self.universal_kernels_surface):
             raise AssertionError("Missing definitions for surface integral")  # problem.py:340-346
         # COO indices (problem.py:86-107)
         fe = self.fe
@@ -168,9 +175,10 @@ class OracleProblem:
         self.shape_vals = torch.from_numpy(fe.shape_vals)
         self.face_data = []
         for b in self.boundary_inds_list:
-            _, nanson = fe.get_face_shape_grads(b)
+            fgrads, nanson = fe.get_face_shape_grads(b)
             self.face_data.append(dict(
                 vals=torch.from_numpy(fe.face_shape_vals[b[:, 1]]),
+                grads=torch.from_numpy(fgrads),
                 nanson=torch.from_numpy(nanson),
                 x=torch.from_numpy(fe.get_physical_surface_quad_points(b)),
                 cells=b[:, 0]))
@@ -189,13 +197,21 @@ class OracleProblem:
             uq = torch.einsum("nv,qn->qv", u, self.shape_vals)
             m = torch.func.vmap(self.mass_map)(uq, x, *iv)
             val = val + torch.einsum("qv,qn,q->nv", m, self.shape_vals, jxw)
+        if self.universal_kernel is not None:   # problem.py:289-294
+            val = val + self.universal_kernel(u_flat, x, grads, jxw[None, :], vgjxw[:, :, None, :],
+                                              *iv).reshape(u.shape)
         return val.reshape(-1)
 
-    def _face_kernel(self, fn, u_flat, fvals, nanson, x, *iv):
+    def _face_kernel(self, fn, ufn, u_flat, fvals, fgrads, nanson, x, *iv):
         u = u_flat.reshape(self.fe.num_nodes, self.vec)
-        uq = torch.einsum("nv,qn->qv", u, fvals)
-        t = torch.func.vmap(fn)(uq, x, *iv)
-        return torch.einsum("qv,qn,q->nv", t, fvals, nanson).reshape(-1)
+        val = torch.zeros_like(u_flat)
+        if fn is not None:
+            uq = torch.einsum("nv,qn->qv", u, fvals)
+            t = torch.func.vmap(fn)(uq, x, *iv)
+            val = val + torch.einsum("qv,qn,q->nv", t, fvals, nanson).reshape(-1)
+        if ufn is not None:                      # problem.py:318-323
+            val = val + ufn(u_flat, x, fvals, fgrads, nanson[None, :]).reshape(-1)
+        return val
 
     def _cells_sol(self, dofs):
         return dofs[torch.from_numpy(self.cell_inds)]
@@ -212,9 +228,10 @@ class OracleProblem:
         cell_val = torch.func.vmap(self._cell_kernel)(*args)
         faces = []
         for i, fd in enumerate(self.face_data):
-            fn = self.surface_maps[i]
-            fargs = (cs[fd["cells"]], fd["vals"], fd["nanson"], fd["x"], *internal_vars_surfaces[i])
-            k = lambda *a, fn=fn: self._face_kernel(fn, *a)
+            fn = self.surface_maps[i] if i < len(self.surface_maps) else None
+            ufn = self.universal_kernels_surface[i] if i < len(self.universal_kernels_surface) else None
+            fargs = (cs[fd["cells"]], fd["vals"], fd["grads"], fd["nanson"], fd["x"], *internal_vars_surfaces[i])
+            k = lambda *a, fn=fn, ufn=ufn: self._face_kernel(fn, ufn, *a)
             fval = torch.func.vmap(k)(*fargs)
             fjac = torch.func.vmap(torch.func.jacfwd(k))(*fargs) if jac else None
             faces.append((fval, fjac))

@@ -1,0 +1,170 @@
+"""Two workloads run exactly as stated:
+
+* Plain FP64 linear elasticity on the 10^3 HEX8 unit cube (1,000 cells, 3,993 dofs), E = 70e3,
+  nu = 0.3, u = 0 on x = 0, traction (0, 0, -100) on x = 1 (surface map (0, 0, +100), the
+  reference's sign convention), one solve to relative residual 1e-12, against the oracle's
+  direct solve -- the mesh of tests/benchmarks/linear_elasticity_cube.
+* SIMP compliance on the 120x60x30 HEX8 cantilever (216,000 cells, 686,433 dofs), theta =
+  0.5 + U(-0.05, 0.05) seeded, p = 3, Emin = 1e-3: the ad_wrapper gradient against the oracle's
+  FP64 adjoint algebra evaluated on the CPU with the same solution, against central finite
+  differences (h = 1e-6) on 20 cells drawn by seed 0, and the mixed path against FP64.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _cube(cuda):
+    import jax_fem_gb300 as jf
+    from oracle import fem as ofem, materials as omat
+    m = jf.box_mesh(10, 10, 10, 1.0, 1.0, 1.0)
+    pts, cells = m.points, m.cells_dict["hexahedron"]
+    x0 = lambda p: np.isclose(p[0], 0.0, atol=1e-5)
+    x1 = lambda p: np.isclose(p[0], 1.0, atol=1e-5)
+    zero = lambda p: 0.0
+    bc = [[x0] * 3, [0, 1, 2], [zero] * 3]
+
+    class P(jf.Problem):
+        def get_tensor_map(self):
+            return jf.LinearElastic(70e3, 0.3)
+
+        def get_surface_maps(self):
+            return [lambda u, x: np.array([0.0, 0.0, 100.0])]
+
+    prob = P(jf.Mesh(pts, cells), vec=3, dim=3, dirichlet_bc_info=bc, location_fns=[x1])
+    oprob = ofem.OracleProblem(pts, cells, 3, dirichlet_bc_info=bc, location_fns=[x1],
+                               tensor_map=omat.linear_elastic(70e3, 0.3),
+                               surface_maps=[lambda u, x: torch.tensor([0.0, 0.0, 100.0], dtype=torch.float64)])
+    return prob, oprob
+
+
+def _bjacobi(A, vec=3):
+    """Inverse 3x3 node blocks of A (CPU), applied as the PCG preconditioner."""
+    n = A.shape[0] // vec
+    D = np.zeros((n, vec, vec))
+    Ad = A.tocsr()
+    for r in range(vec):
+        for c in range(vec):
+            rows = vec * np.arange(n) + r
+            D[:, r, c] = np.asarray(Ad[rows, vec * np.arange(n) + c]).reshape(-1)
+    Dinv = np.linalg.inv(D)
+    return lambda v: np.einsum("nij,nj->ni", Dinv, v.reshape(n, vec)).reshape(-1)
+
+
+def test_config1_cube_fp64_vs_direct_and_pcg_iterates(cuda):
+    """Solution vs the oracle's spsolve within kappa(A) * 1e-12 (the bound a relative residual of
+    1e-12 gives; kappa measured here on the CPU), and the FP64 PCG iterates themselves against the
+    restated PCG (same block-Jacobi preconditioner) after 1, 5 and 25 iterations to 1e-12: the
+    arithmetic of the FP64 path matches the oracle at 1e-12 even where the solution tolerance is
+    bounded by conditioning."""
+    import jax_fem_gb300 as jf
+    from oracle import fem as ofem, solve as osolve
+    prob, oprob = _cube(cuda)
+    eng = prob._engine
+    lin = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}}
+    sol = jf.solver(prob, dict(lin, rel_tol=1e-12, tol=0.0))[0].reshape(-1).cpu().numpy()
+    ref, info = osolve.newton_solve(oprob, {"spsolve_solver": {}, "rel_tol": 1e-12, "tol": 0.0}, return_info=True)
+    ref = np.asarray(ref).reshape(-1)
+    # condition number of the Dirichlet-eliminated system (Lanczos on the CPU)
+    rows, _ = oprob.bc_rows()
+    free = np.setdiff1d(np.arange(oprob.num_total_dofs_all_vars), rows)
+    oprob.newton_update(torch.zeros(oprob.num_total_dofs_all_vars, dtype=torch.float64))
+    K = ofem.assemble_petsc(oprob)
+    Kff = K[free][:, free].tocsc()
+    lmax = spla.eigsh(Kff, k=1, which="LA", return_eigenvectors=False)[0]
+    lmin = spla.eigsh(Kff, k=1, sigma=0.0, which="LM", return_eigenvectors=False)[0]
+    kappa = lmax / lmin
+    err = np.abs(sol - ref).max() / np.abs(ref).max()
+    assert err <= kappa * 1e-12, (err, kappa)
+    assert err <= 1e-10
+    # the PCG iterates: GPU fem_pcg with maxiter k vs the restated PCG on the same matrix and RHS
+    z = torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda)
+    A = eng.tangent(z, jf._lib.FEM_F64, jf._lib.FEM_BC_SYMMETRIC, cache=False)
+    b = -eng.residual(z, apply_bc=True)
+    A_cpu = A.to_scipy()
+    b_cpu = b.cpu().numpy()
+    M = _bjacobi(A_cpu)
+    for k in (1, 5, 25):
+        x = torch.zeros_like(b)
+        eng.krylov("cg", A, b, x, jf._lib.FEM_PC_BJACOBI, 1e-30, 0.0, k)
+        xo, it = osolve.pcg(A_cpu, b_cpu, Minv=M, rtol=1e-30, maxiter=k)
+        assert it == k
+        d = np.abs(x.cpu().numpy() - xo).max() / np.abs(xo).max()
+        assert d <= 1e-12, (k, d)
+
+
+def _cantilever(cuda, n=(120, 60, 30)):
+    import cases
+    prob, _, theta_np = cases.simp_box(*n)
+    return prob, theta_np
+
+
+def _compliance_grad(prob, theta_np, cuda, opts, adj):
+    import jax_fem_gb300 as jf
+    theta = torch.tensor(theta_np, device=cuda, requires_grad=True)
+    fwd = jf.ad_wrapper(prob, opts, adj)
+    sol = fwd(theta)[0]
+    J = torch.dot(prob._engine.f_ext, sol.reshape(-1))
+    J.backward()
+    return sol.detach().reshape(-1), J.item(), theta.grad.detach().cpu().numpy().reshape(-1)
+
+
+def test_config3_simp_120x60x30_gradient(cuda):
+    import jax_fem_gb300 as jf
+    from oracle import fem as ofem, simp_fast
+    prob, theta_np = _cantilever(cuda)
+    eng = prob._engine
+    assert eng.num_cells == 216000 and eng.num_dofs == 686433
+    lin = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-13}}
+    # the PCG tolerance sets the accuracy; Newton (linear problem) takes one step: its relative
+    # residual floors near 4e-12 at 686k dofs in FP64, so rel_tol 1e-10 ends it after that step
+    o64 = dict(lin, rel_tol=1e-10, tol=0.0)
+    u, J, g = _compliance_grad(prob, theta_np, cuda, o64, lin)
+    # oracle on the CPU: the restated assembly (element tangents E(theta) K0_e, PETSc-pattern sum,
+    # symmetric elimination) and the restated adjoint algebra, evaluated with the GPU solution.
+    # R(u) = K u + f (the surface map's load with the reference's sign, f = eng.f_ext), so K u = -f;
+    # J = f.u, the adjoint K lam = f gives lam = -u and dJ/dtheta_e = -lam_e^T E'(theta_e) K0_e u_e
+    # = E'(theta_e) u_e^T K0_e u_e.
+    pts, cells = prob.fes[0].points, prob.fes[0].cells
+    f = eng.f_ext.cpu().numpy()
+    rows = eng.bc_rows_long.cpu().numpy()
+    sc = simp_fast.SimpCantilever(pts, cells, rows, -f)
+    A = sc.assemble_csr(theta_np)
+    uc = u.cpu().numpy()
+    res = np.linalg.norm(sc.f - A @ uc) / np.linalg.norm(sc.f)
+    assert res <= 1e-11, res
+    th = theta_np.reshape(-1)
+    dE = (1.0 - 1e-3) * 3.0 * th ** 2
+    ue = uc[sc.dofs]
+    g_or = dE * np.einsum("ci,cij,cj->c", ue, sc.K0, ue)
+    assert np.abs(g - g_or).max() <= 1e-10 * np.abs(g_or).max()
+    assert abs(J - f @ uc) <= 1e-14 * abs(J)
+    # central finite differences on 20 cells drawn by seed 0
+    rng = np.random.default_rng(0)
+    cells_fd = rng.choice(len(th), size=20, replace=False)
+    h = 1e-6
+    errs = []
+    for c in cells_fd:
+        vals = []
+        for s in (+1, -1):
+            tp = theta_np.copy()
+            tp[c, 0] += s * h
+            prob.set_params(torch.tensor(tp, device=cuda))
+            uu = jf.solver(prob, o64)[0]
+            vals.append(torch.dot(eng.f_ext, uu.reshape(-1)).item())
+        fd = (vals[0] - vals[1]) / (2 * h)
+        errs.append(abs(fd - g[c]))
+    errs = np.asarray(errs)
+    print("config 3 FD: max |fd - g| / max|g| =", errs.max() / np.abs(g).max(),
+          " max relative per cell =", (errs / np.abs(g[cells_fd])).max())
+    assert errs.max() <= 1e-4 * np.abs(g).max()
+    # mixed (DF48 + double-float CG + FP64 reliable updates) against FP64
+    prob.set_params(torch.tensor(theta_np, device=cuda))
+    um, Jm, gm = _compliance_grad(prob, theta_np, cuda, dict(o64, precision="mixed"), dict(lin, precision="mixed"))
+    assert (um - u).abs().max().item() <= 1e-9 * u.abs().max().item()
+    assert abs(Jm - J) <= 1e-10 * abs(J)
+    assert np.abs(gm - g).max() <= 1e-8 * np.abs(g).max()

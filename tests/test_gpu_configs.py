@@ -172,8 +172,9 @@ def test_j2_modulus_field_five_steps_gradient(cuda, n):
     """J2 (E=70e3, nu=0.3, sig0=250) with a per-cell modulus field mu0 * exp(0.2 z - 0.02),
     z ~ N(0,1) seed 0, five load steps of the x=1 face u_x ramp, objective ||u_5 - u_target||^2.
     The gradient (implicit adjoint of every step + reverse mode of every history update) matches
-    central finite differences along a smooth direction to 1e-4 relative (h = 1e-5), on 8^3 and
-    on the full 100^3 (3,090,903 dofs) case."""
+    central finite differences along a smooth direction to 1e-4 relative (h = 1e-5), and along a
+    random per-cell direction the difference quotient's gap closes as h shrinks (h = 1e-3, 2.5e-4,
+    6.25e-5), on 8^3 and on the full 100^3 (3,090,903 dofs) case."""
     prob, bc = _j2_mu_problem(n)
     eng = prob._engine
     g = torch.Generator().manual_seed(0)
@@ -200,6 +201,25 @@ def test_j2_modulus_field_five_steps_gradient(cuda, n):
     fd = (Jp - Jm) / (2 * h)
     an = torch.dot(grad, v).item()
     assert abs(fd - an) <= 1e-4 * max(abs(fd), abs(an)), (fd, an)
+    # A purely random per-cell direction moves many quadrature points across the yield surface,
+    # where the return map has a kink: J along the ray is only piecewise smooth, and a central
+    # difference over [-h, h] carries an error from the kinks inside it that shrinks with h (the
+    # number of points crossing is proportional to h), not the O(h^2) of a smooth function.  A
+    # bias in the adjoint gradient would instead leave a floor.  So the gap must fall at every
+    # 4x step of h over a 16x range and be at least 3x smaller at the smallest h.
+    w = torch.randn(eng.num_cells, generator=g, dtype=torch.float64).to(cuda)
+    an_w = torch.dot(grad, w).item()
+    hs = (1e-3, 2.5e-4, 6.25e-5)
+    gaps = []
+    for hw in hs:
+        with torch.no_grad():
+            Jp = _j2_objective(prob, bc, mu0 + hw * w, disps, u_target, opts).item()
+            Jm = _j2_objective(prob, bc, mu0 - hw * w, disps, u_target, opts).item()
+        gaps.append(abs((Jp - Jm) / (2 * hw) - an_w) / abs(an_w))
+    print(f"J2 n={n}: random direction, relative FD gap " + ", ".join(f"h={hw:g}: {gp:.3e}" for hw, gp in zip(hs, gaps)))
+    assert gaps[1] < gaps[0] and gaps[2] < gaps[1], gaps
+    assert gaps[2] <= gaps[0] / 3, gaps
+    assert gaps[0] <= 5e-2, gaps
 
 
 def test_tet4_pattern_values_solution_vs_oracle(cuda):

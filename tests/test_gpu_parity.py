@@ -267,10 +267,11 @@ def test_simp_adjoint_vs_oracle_and_fd(cuda):
         assert abs(fd - g[c, 0]) <= 1e-5 * np.abs(g).max()
 
 
-@pytest.mark.parametrize("mode", ["mixed", "mixed_sym"])
+@pytest.mark.parametrize("mode", ["mixed", "mixed_sliced", "mixed_sym"])
 def test_mixed_precision_matches_fp64(cuda, mode):
-    """Mixed (DF48 matrix, double-float CG, FP64 reliable updates; with mixed_sym the upper-block
-    DF48 storage) vs FP64: solution, objective, gradient."""
+    """Mixed (DF48 matrix, double-float CG, FP64 reliable updates) vs FP64: solution, objective,
+    gradient.  On this box mesh 'mixed' runs on the structured symmetric storage, 'mixed_sliced'
+    on the general sliced one, 'mixed_sym' on the upper-block storage of the general pattern."""
     import cases
     prob, _, theta_np = cases.simp_box(12, 6, 3)
     o64 = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}, "rel_tol": 1e-12, "tol": 0.0}
@@ -278,7 +279,11 @@ def test_mixed_precision_matches_fp64(cuda, mode):
     a64 = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}}
     amx = dict(a64, precision=mode)
     s64, J64, g64 = _simp_grad(prob, theta_np, cuda, o64, a64)
+    eng = prob._engine
+    eng.solve_log.clear()
     smx, Jmx, gmx = _simp_grad(prob, theta_np, cuda, omx, amx)
+    want = {"mixed": "ssym-df48+fp64", "mixed_sliced": "df48+fp64", "mixed_sym": "sym-df48+fp64"}[mode]
+    assert all(r["precision"] == want for r in eng.solve_log if r["method"] == "cg-refined"), eng.solve_log
     assert (smx - s64).abs().max().item() <= 1e-9 * s64.abs().max().item()
     assert abs(Jmx - J64) <= 1e-10 * abs(J64)
     assert np.abs(gmx - g64).max() <= 1e-8 * np.abs(g64).max()
@@ -503,7 +508,7 @@ def test_df48_spmv_matches_fp64(cuda):
     y64 = A64.matvec(x)
     L = jf._lib
     for fmt, tol in ((L.FEM_DF48, 1e-11), (L.FEM_SLICED_DF48, 1e-11), (L.FEM_SYM_DF48, 1e-11),
-                     (L.FEM_SLICED_F64, 1e-14),
+                     (L.FEM_SSYM_DF48, 1e-11), (L.FEM_SLICED_F64, 1e-14),
                      (L.FEM_SLICED_F32, 1e-6)):
         A = eng.tangent(z, fmt, jf._lib.FEM_BC_SYMMETRIC, cache=False)
         y = A.matvec(x).double()
@@ -532,14 +537,18 @@ def _df_nodes(x, vec):
     return xp
 
 
-@pytest.mark.parametrize("sym", [False, True])
-@pytest.mark.parametrize("n", [(10, 5, 3), (64, 40, 40)])
-def test_spmv_dfx_matches_fp64(cuda, n, sym):
+@pytest.mark.parametrize("kind", ["sliced", "sym", "ssym"])
+@pytest.mark.parametrize("n", [(10, 5, 3), (64, 40, 40), (1, 1, 1), (3, 40, 2), (2, 2, 60), (100, 50, 25)])
+def test_spmv_dfx_matches_fp64(cuda, n, kind):
     """The mixed CG's SpMV (bulk-copy staged, double-float in and out) against the FP64 SpMV:
     y to 1e-11 of max|y|, the fused dot x.y to 1e-11 relative.  (64, 40, 40) has more slices
     than resident warps, so warps stream several slices through their shared-memory ring.  With
     sym the matrix is FEM_SYM_DF48 (upper node blocks; the transposed half through FP64 atomics,
-    the dot through x.Ax = 2 x.(upper part) - x.diag)."""
+    the dot through x.Ax = 2 x.(upper part) - x.diag); with ssym FEM_SSYM_DF48 (structured grid
+    stencil, transposed half in registers and shuffles, plane i+1 and warp edges by atomics).
+    The grids cover one group of lines with a partial warp (1,1,1), more lines per plane than a
+    warp (3,40,2: 41 lines of a plane span two warps), one k step per work item (2,2,60: every row
+    next to a chunk boundary) and items of several steps (64,40,40 and 100,50,25)."""
     import ctypes as C
     import jax_fem_gb300 as jf
     import cases
@@ -549,8 +558,9 @@ def test_spmv_dfx_matches_fp64(cuda, n, sym):
     eng = prob._engine
     z = torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda)
     A64 = eng.tangent(z, L.FEM_F64, L.FEM_BC_SYMMETRIC, cache=False)
-    fmt = L.FEM_SYM_DF48 if sym else L.FEM_SLICED_DF48
+    fmt = {"sliced": L.FEM_SLICED_DF48, "sym": L.FEM_SYM_DF48, "ssym": L.FEM_SSYM_DF48}[kind]
     Adf = eng.tangent(z, fmt, L.FEM_BC_SYMMETRIC, cache=False)
+    assert Adf.precision == fmt
     g = torch.Generator(device=cuda).manual_seed(3)
     x = torch.randn(eng.num_dofs, dtype=torch.float64, device=cuda, generator=g)
     y64 = A64.matvec(x)
