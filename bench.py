@@ -246,6 +246,8 @@ def traffic_from_profile(n_units, kind="df48"):
     """DRAM bytes (read + write) per DF48 SpMV launch: the committed ncu summary's bytes per
     nonzero (of the full matrix) on a smaller case, scaled to this workload's nnz (traffic grows
     with nnz)."""
+    if kind not in TRAFFIC_PROFILES:
+        return None
     try:
         with open(TRAFFIC_PROFILES[kind]) as f:
             for line in f:

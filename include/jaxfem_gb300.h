@@ -329,8 +329,8 @@ int fem_pcg(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t prec
  * forbid allocation after start-up.  Its scratch is a fixed file-scope device array of
  * about 8.6 MB that every GPU loading the library keeps until the process exits; systems of
  * more than 262144 dofs (n_nodes*vec) are rejected with FEM_ERR_CAPACITY.  The first call on a
- * device looks up the array's device address and caches it for that device (make that first
- * call before any stream capture).  The cached address belongs to the CUDA context of that
+ * device looks up the array's device address and caches it for that device.  The cached
+ * address belongs to the CUDA context of that
  * first call: after cudaDeviceReset on a device, the next call would hand the kernels a stale
  * address, so a process that resets a device must not call this entry point on it again.
  * Every call shares the array, so calls that overlap on the GPU (two streams, two threads)

@@ -2061,9 +2061,9 @@ static int launch_dfdf(const fem_pattern_t* pat, int64_t n_nodes, const float* v
 }
 
 // The structured symmetric SpMV (FEM_SSYM_DF48).  Work items are (group of 32 lines, k range);
-// the number of k ranges per group is chosen so that the items fill the resident warps with the
-// fewest rounds of the longest item (a partly filled last round costs a whole item's time).
-// Grid: min(items, resident warps) warps.  Needs 16-byte aligned values and corrections.
+// the groups are cut into as few k ranges as fill the resident warps in one round (every cut adds
+// boundary rows whose transposed parts go through atomics).  Grid: min(items, resident warps)
+// warps.  Needs 16-byte aligned values and corrections.
 static int launch_ssym(const fem_pattern_t* pat, const float* vhi, const int16_t* vlo, const float2* xp, float* yh,
                        float* yl, double* qT, KCtl* C, int op, double* partials, cudaStream_t s) {
   if (!(aligned16(vhi) && aligned16(vlo) && qT))
@@ -2080,14 +2080,8 @@ static int launch_ssym(const fem_pattern_t* pat, const float* vhi, const int16_t
   }
   const int64_t resident = (int64_t)sm_count() * per_sm * SS_WARPS;
   const SsGrid G0 = ss_grid(pat, 1);
-  int best = 1;
-  int64_t best_cost = INT64_MAX;
-  for (int c = 1; c <= (int)std::min<int64_t>(G0.nz, 64); ++c) {
-    const int64_t rounds = (G0.groups * c + resident - 1) / resident;
-    const int64_t cost = rounds * ((G0.nz + c - 1) / c);
-    if (cost < best_cost) { best_cost = cost; best = c; }
-  }
-  const SsGrid G = ss_grid(pat, best);
+  const int chunks = (int)std::max<int64_t>(1, std::min<int64_t>(G0.nz, resident / std::max<int64_t>(G0.groups, 1)));
+  const SsGrid G = ss_grid(pat, chunks);
   int64_t warps = std::min<int64_t>(G.groups * G.chunks, resident);
   int64_t g = (warps + SS_WARPS - 1) / SS_WARPS;
   if (g > MAX_PARTIAL_BLOCKS) g = MAX_PARTIAL_BLOCKS;
@@ -3042,7 +3036,7 @@ constexpr size_t STATIC_PCG_BYTES = al_c(sizeof(KCtl)) + al_c(sizeof(double) * 3
 __device__ __align__(256) unsigned char g_static_pcg_scratch[STATIC_PCG_BYTES];
 
 // Device address of the scratch array on the current device, looked up once per device
-// (on the first call there, which should come before any stream capture).  The host-side
+// (on the first call there).  The host-side
 // name g_static_pcg_scratch is only a stand-in for the symbol and is never passed to a
 // kernel.  The cached address belongs to the context of that first call; it is not
 // looked up again, so it does not survive a cudaDeviceReset of the device.

@@ -25,7 +25,7 @@ namespace fem {
 
 constexpr int SS_SLOTS = 14;
 constexpr int SS_WARPS = 4;
-constexpr int SS_STAGES = 3;
+constexpr int SS_STAGES = 2;           // ring depth per warp (2 x 3456 B in flight)
 constexpr int SS_STAGE_SLOTS = 2;          // 14 slots per row step = 7 stages
 constexpr int SS_WIN_LINES = 67;           // 33 own lines (L0 .. L0+32) + 34 far (L0+ny-1 .. L0+ny+32)
 
@@ -156,17 +156,31 @@ __device__ __forceinline__ double f2d_bits(float f) {
   return __longlong_as_double((long long)d);
 }
 
-// qT[c][node] += h + l (component stride qt_stride); one FP64 add per nonzero component
+// qT[c][node] += h + l (component stride qt_stride).  For emissions made by every lane of a warp:
+// one FP64 add per nonzero component (a warp-wide FP64 instruction serves 32 rows).
 __device__ __forceinline__ void ss_atomic3(double* qT, int64_t stride, int64_t node, const float* h, const float* l) {
 #pragma unroll
   for (int c = 0; c < 3; ++c)
     if ((__float_as_uint(h[c]) & 0x7FFFFFFFu) != 0u) atomicAdd(qT + (int64_t)c * stride + node, f2d_bits(h[c]) + f2d_bits(l[c]));
 }
 
+// The same for emissions made by a single lane (the warp's edge lanes): h and l as two atomics and
+// no FP64 arithmetic -- a warp-wide FP64 instruction would cost GB300's FP64 pipe as much for one
+// active lane as for 32.
+__device__ __forceinline__ void ss_atomic3_lane(double* qT, int64_t stride, int64_t node, const float* h,
+                                                const float* l) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    if ((__float_as_uint(h[c]) & 0x7FFFFFFFu) != 0u) {
+      atomicAdd(qT + (int64_t)c * stride + node, f2d_bits(h[c]));
+      if ((__float_as_uint(l[c]) & 0x7FFFFFFFu) != 0u) atomicAdd(qT + (int64_t)c * stride + node, f2d_bits(l[c]));
+    }
+}
+
 // y (double-float, the row parts plus the transposed parts that stayed in the warp) and qT (FP64,
 // the rest, added by atomics) with y + qT = A x; fused dot x.(A x) = sum_i 2 x_i.(U x)_i - x_i.A_ii x_i
 // (U: the stored upper blocks including the diagonal).  Requires 16-byte aligned vals and vlo.
-__global__ void __launch_bounds__(SS_WARPS * 32)
+__global__ void __launch_bounds__(SS_WARPS * 32, 4)   // 4 CTAs (16 warps) per SM
 spmv_ssym_bulk_kernel(SsGrid G, const float* __restrict__ vals, const int16_t* __restrict__ vlo,
                       const float2* __restrict__ xp, float* __restrict__ yh, float* __restrict__ yl,
                       double* __restrict__ qT, KCtl* C, int op, double* partials) {
@@ -268,19 +282,23 @@ spmv_ssym_bulk_kernel(SsGrid G, const float* __restrict__ vals, const int16_t* _
     int pm = (int)((k0 + 2) % 3), p0 = (int)(k0 % 3), pp = (int)((k0 + 1) % 3);   // rows k-1, k, k+1
     load_win(L0, k0 - 1, pm);
     load_win(L0, k0, p0);
-    Df3<3> Y[3], F[3];   // own line rows k-1, k, k+1; far line rows k-1, k, k+1
+    Df3<3> Y0, Y1, Y2, F0, F1, F2;   // own line rows k-1, k, k+1; far line rows k-1, k, k+1
 #pragma unroll
-    for (int q = 0; q < 3; ++q)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) { Y[q].h[c] = Y[q].l[c] = F[q].h[c] = F[q].l[c] = 0.f; }
+    for (int c = 0; c < 3; ++c) {
+      Y0.h[c] = Y0.l[c] = Y1.h[c] = Y1.l[c] = Y2.h[c] = Y2.l[c] = 0.f;
+      F0.h[c] = F0.l[c] = F1.h[c] = F1.l[c] = F2.h[c] = F2.l[c] = 0.f;
+    }
     for (int64_t k = k0; k < k1 && !fault; ++k) {
       load_win(L0, k + 1, pp);
       __syncwarp();
       float xh[3], xl[3];   // the row's own x
       get_win(lane, p0, xh, xl);
-      float rh[3] = {0.f, 0.f, 0.f}, rl[3] = {0.f, 0.f, 0.f};   // row part (U x)_row
+      // row part (U x)_row in two banks (the two slots of a stage), two independent chains
+      float rh[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}}, rl[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
       float dh = 0.f, dl = 0.f;                                  // x.A_ii x
-#pragma unroll
+      // The seven stages of a row step share one loop body (kept rolled: unrolling all 14 slots
+      // overflowed the instruction cache); slot-dependent routing is warp-uniform branching.
+#pragma unroll 1
       for (int sp = 0; sp < SS_SLOTS / SS_STAGE_SLOTS; ++sp) {
         const bool ok = mbar_wait(bars + stage, (parity >> stage) & 1u);
         if (!__all_sync(0xffffffffu, ok)) { fault = true; break; }
@@ -300,19 +318,15 @@ spmv_ssym_bulk_kernel(SsGrid G, const float* __restrict__ vals, const int16_t* _
           }
           // neighbour x of this slot from the window
           const int dk = ss_dk(s);
-          int w;
-          if (s == 0 || s == 1) w = lane;
-          else if (s < 5) w = lane + 1;
-          else w = 33 + lane + 1 + ss_dj(s);
+          const bool far = s >= 5;
+          const int dj = far ? ss_dj(s) : 1;
+          const int w = s < 2 ? lane : far ? 33 + lane + 1 + dj : lane + 1;
           float nh[3], nl[3];
           get_win(w, dk < 0 ? pm : dk > 0 ? pp : p0, nh, nl);
 #pragma unroll
-          for (int v = 0; v < 9; ++v) {
-            const int r = v / 3, d = v % 3;
-            df_acc(rh[r], rl[r], df2{ah[v], al[v]}, df2{nh[d], nl[d]});
-          }
+          for (int v = 0; v < 9; ++v) df_acc(rh[u][v / 3], rl[u][v / 3], df2{ah[v], al[v]}, df2{nh[v % 3], nl[v % 3]});
+          float th[3] = {0.f, 0.f, 0.f}, tl[3] = {0.f, 0.f, 0.f};
           if (s == 0) {   // x.A_ii x for the fused dot
-            float th[3] = {0.f, 0.f, 0.f}, tl[3] = {0.f, 0.f, 0.f};
 #pragma unroll
             for (int v = 0; v < 9; ++v) df_acc(th[v / 3], tl[v / 3], df2{ah[v], al[v]}, df2{xh[v % 3], xl[v % 3]});
 #pragma unroll
@@ -320,47 +334,50 @@ spmv_ssym_bulk_kernel(SsGrid G, const float* __restrict__ vals, const int16_t* _
             continue;
           }
           // transposed contribution t = A^T x_row to the slot's neighbour
-          float th[3] = {0.f, 0.f, 0.f}, tl[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-          for (int v = 0; v < 9; ++v) {
-            const int r = v / 3, d = v % 3;
-            df_acc(th[d], tl[d], df2{ah[v], al[v]}, df2{xh[r], xl[r]});
-          }
+          for (int v = 0; v < 9; ++v) df_acc(th[v % 3], tl[v % 3], df2{ah[v], al[v]}, df2{xh[v / 3], xl[v / 3]});
 #pragma unroll
           for (int c = 0; c < 3; ++c) { const df2 f = df_fast(th[c], tl[c]); th[c] = f.h; tl[c] = f.l; }
-          if (s == 1) {                       // own line, row k+1
-            df3_add(Y[2].h, Y[2].l, th, tl);
-          } else if (s < 5) {                 // line L+1, row k+dk: lane l+1's rows
-            float uh[3], ul[3];
+          if (s == 1) {                        // own line, row k+1
+            df3_add(Y2.h, Y2.l, th, tl);
+            continue;
+          }
+          // line L+1 (slots 2-4) and plane i+1 lines L+ny+dj (slots 5-13): the receiving lane is
+          // lane+1 (shuffle up) for the next line and dj = +1, lane-1 (shuffle down) for dj = -1,
+          // the lane itself for dj = 0
+          float uh[3], ul[3];
+          bool recv = true;
+          if (dj > 0) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) { uh[c] = df_shfl_up_f(th[c]); ul[c] = df_shfl_up_f(tl[c]); }
-            if (lane > 0) df3_add(Y[1 + dk].h, Y[1 + dk].l, uh, ul);
-            if (lane == 31 && lv) {
-              const int64_t tk = k + dk, tline = L0 + 32;
-              if (tline < G.nl && tk >= 0 && tk < G.nz) ss_atomic3(qT, qstride, tline * G.nz + tk, th, tl);
-            }
-          } else {                            // plane i+1: far line L0+ny+lane+dj, row k+dk
-            const int dj = ss_dj(s);
-            float uh[3], ul[3];
-            if (dj == 0) {
-              df3_add(F[1 + dk].h, F[1 + dk].l, th, tl);
-            } else if (dj < 0) {              // lane m gets lane m+1's contribution
+            recv = lane > 0;
+          } else if (dj < 0) {
 #pragma unroll
-              for (int c = 0; c < 3; ++c) { uh[c] = df_shfl_down_f(th[c]); ul[c] = df_shfl_down_f(tl[c]); }
-              if (lane < 31) df3_add(F[1 + dk].h, F[1 + dk].l, uh, ul);
-              if (lane == 0 && lv) {        // far line L0+ny-1: outside this warp's far lines
-                const int64_t tk = k + dk, tline = L0 + G.ny - 1;
-                if (tline < G.nl && tk >= 0 && tk < G.nz) ss_atomic3(qT, qstride, tline * G.nz + tk, th, tl);
-              }
-            } else {                          // lane m gets lane m-1's contribution
+            for (int c = 0; c < 3; ++c) { uh[c] = df_shfl_down_f(th[c]); ul[c] = df_shfl_down_f(tl[c]); }
+            recv = lane < 31;
+          } else {
 #pragma unroll
-              for (int c = 0; c < 3; ++c) { uh[c] = df_shfl_up_f(th[c]); ul[c] = df_shfl_up_f(tl[c]); }
-              if (lane > 0) df3_add(F[1 + dk].h, F[1 + dk].l, uh, ul);
-              if (lane == 31 && lv) {       // far line L0+ny+32
-                const int64_t tk = k + dk, tline = L0 + G.ny + 32;
-                if (tline < G.nl && tk >= 0 && tk < G.nz) ss_atomic3(qT, qstride, tline * G.nz + tk, th, tl);
-              }
-            }
+            for (int c = 0; c < 3; ++c) { uh[c] = th[c]; ul[c] = tl[c]; }
+          }
+          if (!recv) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) uh[c] = ul[c] = 0.f;
+          }
+          if (far) {
+            if (dk < 0) df3_add(F0.h, F0.l, uh, ul);
+            else if (dk == 0) df3_add(F1.h, F1.l, uh, ul);
+            else df3_add(F2.h, F2.l, uh, ul);
+          } else {
+            if (dk < 0) df3_add(Y0.h, Y0.l, uh, ul);
+            else if (dk == 0) df3_add(Y1.h, Y1.l, uh, ul);
+            else df3_add(Y2.h, Y2.l, uh, ul);
+          }
+          // the edge lane whose target line lies outside this warp's lines: an atomic
+          const int esc = dj > 0 ? 31 : dj < 0 ? 0 : -1;
+          if (lane == esc && lv) {
+            const int64_t tk = k + dk;
+            const int64_t tline = !far ? L0 + 32 : dj < 0 ? L0 + G.ny - 1 : L0 + G.ny + 32;
+            if (tline < G.nl && tk >= 0 && tk < G.nz) ss_atomic3_lane(qT, qstride, tline * G.nz + tk, th, tl);
           }
         }
         __syncwarp();
@@ -372,11 +389,11 @@ spmv_ssym_bulk_kernel(SsGrid G, const float* __restrict__ vals, const int16_t* _
       float yr[3], yrl[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const df2 f = df_fast(rh[c], rl[c]);
+        const df2 f = df_add(df_fast(rh[0][c], rl[0][c]), df_fast(rh[1][c], rl[1][c]));
         yr[c] = f.h;
         yrl[c] = f.l;
       }
-      df3_add(Y[1].h, Y[1].l, yr, yrl);
+      df3_add(Y1.h, Y1.l, yr, yrl);
       if (lv) {
         float eh = 0.f, el = 0.f;
 #pragma unroll
@@ -394,21 +411,21 @@ spmv_ssym_bulk_kernel(SsGrid G, const float* __restrict__ vals, const int16_t* _
         if (kp >= k0) {
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            const df2 f = df_fast(Y[0].h[c], Y[0].l[c]);
+            const df2 f = df_fast(Y0.h[c], Y0.l[c]);
             yh[3 * node + c] = f.h;
             yl[3 * node + c] = f.l;
           }
         } else {
-          ss_atomic3(qT, qstride, node, Y[0].h, Y[0].l);
+          ss_atomic3(qT, qstride, node, Y0.h, Y0.l);
         }
       }
       // far row k-1 complete (for this warp's sources): one atomic per component
-      if (fv && kp >= 0) ss_atomic3(qT, qstride, Lf * G.nz + kp, F[0].h, F[0].l);
-      Y[0] = Y[1]; Y[1] = Y[2];
-      F[0] = F[1]; F[1] = F[2];
+      if (fv && kp >= 0) ss_atomic3(qT, qstride, Lf * G.nz + kp, F0.h, F0.l);
+      Y0 = Y1; Y1 = Y2;
+      F0 = F1; F1 = F2;
       { const int t = pm; pm = p0; p0 = pp; pp = t; }
 #pragma unroll
-      for (int c = 0; c < 3; ++c) { Y[2].h[c] = Y[2].l[c] = F[2].h[c] = F[2].l[c] = 0.f; }
+      for (int c = 0; c < 3; ++c) { Y2.h[c] = Y2.l[c] = F2.h[c] = F2.l[c] = 0.f; }
       __syncwarp();   // window slots of position k-1 are overwritten by the next step's load
     }
     if (fault) break;
@@ -417,15 +434,15 @@ spmv_ssym_bulk_kernel(SsGrid G, const float* __restrict__ vals, const int16_t* _
       const int64_t node = L * G.nz + (k1 - 1);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const df2 f = df_fast(Y[0].h[c], Y[0].l[c]);
+        const df2 f = df_fast(Y0.h[c], Y0.l[c]);
         yh[3 * node + c] = f.h;
         yl[3 * node + c] = f.l;
       }
-      if (k1 < G.nz) ss_atomic3(qT, qstride, L * G.nz + k1, Y[1].h, Y[1].l);
+      if (k1 < G.nz) ss_atomic3(qT, qstride, L * G.nz + k1, Y1.h, Y1.l);
     }
     if (fv) {
-      ss_atomic3(qT, qstride, Lf * G.nz + (k1 - 1), F[0].h, F[0].l);
-      if (k1 < G.nz) ss_atomic3(qT, qstride, Lf * G.nz + k1, F[1].h, F[1].l);
+      ss_atomic3(qT, qstride, Lf * G.nz + (k1 - 1), F0.h, F0.l);
+      if (k1 < G.nz) ss_atomic3(qT, qstride, Lf * G.nz + k1, F1.h, F1.l);
     }
   }
   if (fault) {

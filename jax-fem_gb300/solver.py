@@ -6,11 +6,12 @@ Mirrors jax_fem/solver.py (Newton branch, 63-553 and 1079-1455):
     dict) with tol / rel_tol / line_search_flag / initial_guess and a 'linear'
     block naming jax_solver / petsc_solver / spsolve_solver / custom_solver.
     Additional keys: 'precision' ('fp64' default; 'mixed': CG on a DF48 copy of
-    the FP64 tangent with double-float vectors and FP64 reliable updates;
-    on a structured box grid of HEX8/TET4 nodes 'mixed' stores only the diagonal
-    and upper stencil blocks (FEM_SSYM_DF48); 'mixed_sliced' keeps the general
-    sliced DF48 copy there too; 'mixed_sym': upper-block storage of a general
-    pattern with the transposed half by FP64 atomics; 'mixed32': FP32 matrix and
+    the FP64 tangent (sliced storage) with double-float vectors and FP64
+    reliable updates; 'mixed_sliced' is the same; 'mixed_ssym': on a structured
+    box grid of nodes, only the diagonal and upper stencil blocks
+    (FEM_SSYM_DF48, half the matrix bytes, slower on GB300: issue bound);
+    'mixed_sym': upper-block storage of a general pattern with the transposed
+    half by FP64 atomics; 'mixed32': FP32 matrix and
     vectors with FP64 reliable updates -- BiCGStab under a mixed precision runs
     in FP32 and Newton's FP64 residual refines it), 'inner_rtol' (that
     BiCGStab's tolerance), 'refine_delta', 'max_iter' (Newton cap).
@@ -108,25 +109,27 @@ def resolve_linear(linear_options):
 
 def _precision(cfg):
     p = cfg.get("precision", "fp64")
-    if p not in ("fp64", "mixed", "mixed_sliced", "mixed_sym", "mixed32"):
-        raise ValueError("precision must be 'fp64', 'mixed' (DF48 matrix, double-float vectors), 'mixed_sliced' "
-                         "(the same, general sliced storage on every mesh), 'mixed_sym' (the same "
-                         "with upper-block DF48 storage) or 'mixed32' (FP32)")
+    if p not in ("fp64", "mixed", "mixed_sliced", "mixed_ssym", "mixed_sym", "mixed32"):
+        raise ValueError("precision must be 'fp64', 'mixed' or 'mixed_sliced' (sliced DF48 matrix, double-float "
+                         "vectors), 'mixed_ssym' (the same with structured symmetric stencil storage on a box "
+                         "grid), 'mixed_sym' (upper-block DF48 storage of a general pattern) or 'mixed32' (FP32)")
     return p
 
 
 def _mixed_matrix_precision(precision, eng=None):
-    """Solver copy of the tangent.  'mixed': the structured symmetric DF48 layout (diagonal and
-    upper stencil blocks, implicit columns; the transposed half in registers and warp shuffles)
-    when the nodes form a box grid (eng.grid) and the tangent is symmetric, sliced DF48 otherwise;
-    'mixed_sliced': sliced DF48 always; 'mixed_sym': upper node blocks of the general pattern with
-    the transposed half through FP64 atomics (slower on GB300: the atomics cost more than the
-    bytes saved); sliced FP32 for 'mixed32'."""
+    """Solver copy of the tangent.  'mixed' / 'mixed_sliced': sliced DF48 (the fastest measured on
+    GB300: the SpMV streams at ~0.89 of the copy peak); 'mixed_ssym': the structured symmetric DF48
+    layout (diagonal and upper stencil blocks, implicit columns; the transposed half in registers
+    and warp shuffles) when the nodes form a box grid (eng.grid) and the tangent is symmetric,
+    sliced DF48 otherwise -- it moves 0.58x the bytes but its double-float arithmetic is issue
+    bound (456 us against 277 us per SpMV at 1M cells); 'mixed_sym': upper node blocks of the
+    general pattern with the transposed half through FP64 atomics (slower on GB300: the atomics
+    cost more than the bytes saved); sliced FP32 for 'mixed32'."""
     if precision == "mixed_sym" and eng is not None and eng.vec == 3 and getattr(eng._mat, "symmetric", False):
         return _lib.FEM_SYM_DF48
-    if precision == "mixed" and eng is not None and eng.grid is not None and eng.tangent_symmetric:
+    if precision == "mixed_ssym" and eng is not None and eng.grid is not None and eng.tangent_symmetric:
         return _lib.FEM_SSYM_DF48
-    if precision in ("mixed", "mixed_sym", "mixed_sliced"):
+    if precision in ("mixed", "mixed_sym", "mixed_sliced", "mixed_ssym"):
         return _lib.FEM_SLICED_DF48
     return _lib.FEM_SLICED_F32
 

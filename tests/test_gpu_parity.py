@@ -267,11 +267,11 @@ def test_simp_adjoint_vs_oracle_and_fd(cuda):
         assert abs(fd - g[c, 0]) <= 1e-5 * np.abs(g).max()
 
 
-@pytest.mark.parametrize("mode", ["mixed", "mixed_sliced", "mixed_sym"])
+@pytest.mark.parametrize("mode", ["mixed", "mixed_ssym", "mixed_sym"])
 def test_mixed_precision_matches_fp64(cuda, mode):
     """Mixed (DF48 matrix, double-float CG, FP64 reliable updates) vs FP64: solution, objective,
-    gradient.  On this box mesh 'mixed' runs on the structured symmetric storage, 'mixed_sliced'
-    on the general sliced one, 'mixed_sym' on the upper-block storage of the general pattern."""
+    gradient.  'mixed' runs on the general sliced storage, 'mixed_ssym' on this machine mesh's
+    structured symmetric storage, 'mixed_sym' on the upper-block storage of the general pattern."""
     import cases
     prob, _, theta_np = cases.simp_box(12, 6, 3)
     o64 = {"petsc_solver": {"ksp_type": "cg", "pc_type": "bjacobi", "rtol": 1e-12}, "rel_tol": 1e-12, "tol": 0.0}
@@ -282,7 +282,7 @@ def test_mixed_precision_matches_fp64(cuda, mode):
     eng = prob._engine
     eng.solve_log.clear()
     smx, Jmx, gmx = _simp_grad(prob, theta_np, cuda, omx, amx)
-    want = {"mixed": "ssym-df48+fp64", "mixed_sliced": "df48+fp64", "mixed_sym": "sym-df48+fp64"}[mode]
+    want = {"mixed": "df48+fp64", "mixed_ssym": "ssym-df48+fp64", "mixed_sym": "sym-df48+fp64"}[mode]
     assert all(r["precision"] == want for r in eng.solve_log if r["method"] == "cg-refined"), eng.solve_log
     assert (smx - s64).abs().max().item() <= 1e-9 * s64.abs().max().item()
     assert abs(Jmx - J64) <= 1e-10 * abs(J64)
