@@ -451,7 +451,7 @@ def kernel_shares(args):
     th0 = theta_init(prob.num_cells).cuda()
     with profile(activities=[ProfilerActivity.CUDA]):
         torch.ones(8, device="cuda").sum().item()     # CUPTI start-up outside the traced step
-    for prec in ("mixed", "fp64"):
+    for prec in (args.precision, "fp64"):
         fwd_o, adj_o = options(prec)
         fwd = jf.ad_wrapper(prob, fwd_o, adj_o)
         run_steps(prob, fwd, theta_step(th0, 0))
@@ -691,6 +691,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, nargs=3, default=list(DEFAULT_SIZE))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed_ssym", "mixed_sym"],
+                    help="mixed-precision variant of the headline run (solver copy of the tangent)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--widened", action="store_true",
@@ -772,7 +774,7 @@ def main():
     # ---- mixed (headline) ------------------------------------------------------
     spmv_in_loop = {}
     with ClockSampler(local) as clk:
-        t_mx, (J_mx, g_mx, u_mx), launches, its_mx, phases_mx = timed("mixed", args.steps, args.warmup,
+        t_mx, (J_mx, g_mx, u_mx), launches, its_mx, phases_mx = timed(args.precision, args.steps, args.warmup,
                                                                        spmv_timer=True)
     clocks = clk.summary()
     roof = spmv_roofline(prob, peak)
@@ -789,7 +791,7 @@ def main():
                                          "gradient": rel(g_mx, g_64)}}
 
     # ---- e2e through the public API with host buffers ----------------------------
-    fwd_opts, adj_opts = options("mixed")
+    fwd_opts, adj_opts = options(args.precision)
     fwd = jf.ad_wrapper(prob, fwd_opts, adj_opts)
     theta_hosts = [theta_step(theta_init(cells), 2000 + k).pin_memory() for k in range(args.steps)]
     grad_host = torch.empty_like(theta_hosts[0]).pin_memory()
@@ -833,7 +835,7 @@ def main():
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 assembly; DF48 matrix (fp32 hi + int16 lo) with double-float SpMV on fp32 pipes; double-float (fp32 pair) CG vectors, f64 dot finish and reliable updates",
         "data": "synthetic",
-        "config": {"workload": name, "precision": "mixed", "tolerance": RTOL,
+        "config": {"workload": name, "precision": args.precision, "tolerance": RTOL,
                    "solver": "block-Jacobi PCG, DF48 SpMV + double-float CG vectors, FP64 reliable updates (true residual)",
                    "l2": "inputs larger than L2 (the DF48 matrix alone is 1.5 GB > 129 MB)",
                    "replicas": "one independent problem per GPU (no data-path collective)"},
