@@ -228,6 +228,56 @@ def spmv_roofline(prob, peak):
     return out
 
 
+def assembly_roofline(prob, peak):
+    """Time the assembly launches with CUDA events on the launching stream (direct C-ABI calls,
+    5 launches each after 2 warm-ups, output zeroed outside the bracket): the double-float matrix
+    (fem_assemble FEM_OUT_MATRIX with FEM_DF48, the mixed path's), the FP64 matrix (the FP64
+    path's) and the FP64 residual, each with the cached geometry.  Algorithmic bytes per launch:
+    per cell its connectivity (4 B per node), slot table (1 B per node pair), cached shape
+    gradients and JxW (8 B x nq x (3 nn + 1)) and qp parameter (8 B x nq); the matrix launches
+    read and write every CSR value once (16 B per nonzero) and read the row pointers; the
+    residual launch reads u and reads and writes the residual (8 B x 3 per dof)."""
+    import ctypes as C
+    import torch
+    import jax_fem_gb300 as jf
+    from jax_fem_gb300._lib import call, ptr, stream_handle
+    eng = prob._engine
+    L_ = jf._lib
+    if eng.shape_grads is None:
+        return None
+    eng.refresh_bc()
+    _, ms = eng.material()
+    cells, nq, nn, nd = eng.num_cells, eng.num_quads, eng.nn, eng.num_dofs
+    per_cell = 4 * nn + nn * nn + 8 * nq * (3 * nn + 1) + 8 * nq
+    u = torch.zeros(nd, dtype=torch.float64, device="cuda")
+    vals = torch.zeros(eng.nnz, dtype=torch.float64, device="cuda")
+    res = torch.zeros(nd, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream()
+    out = {}
+    cases = (("matrix_df48", L_.FEM_OUT_MATRIX, L_.FEM_DF48, cells * per_cell + 16 * eng.nnz + 8 * (nd + 1) + nd),
+             ("matrix_fp64", L_.FEM_OUT_MATRIX, L_.FEM_F64, cells * per_cell + 16 * eng.nnz + 8 * (nd + 1) + nd),
+             ("residual_fp64", L_.FEM_OUT_RESIDUAL, L_.FEM_F64, cells * per_cell + 24 * nd + nd))
+    for name, outputs, prec, algo in cases:
+        def launch():
+            call("fem_assemble", C.byref(eng.mesh), C.byref(ms), C.byref(eng.pattern), outputs, prec, ptr(u), None,
+                 ptr(eng.bc_mask), L_.FEM_BC_SYMMETRIC, ptr(res), ptr(vals), None, stream_handle())
+        ts = []
+        for k in range(7):
+            vals.zero_()
+            res.zero_()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record(s)
+            launch()
+            ev[1].record(s)
+            torch.cuda.synchronize()
+            if k >= 2:
+                ts.append(ev[0].elapsed_time(ev[1]) / 1e3)
+        t = float(np.median(ts))
+        out[name] = {"seconds": t, "algorithmic_bytes": int(algo), "achieved_gbs": algo / t / 1e9,
+                     "frac": algo / t / 1e9 / peak}
+    return out
+
+
 def measured_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -778,6 +828,7 @@ def main():
                                                                        spmv_timer=True)
     clocks = clk.summary()
     roof = spmv_roofline(prob, peak)
+    asm_roof = assembly_roofline(prob, peak)
 
     # ---- plain FP64 ------------------------------------------------------------
     fp64 = None
@@ -833,13 +884,16 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_mx / args.steps * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 assembly; DF48 matrix (fp32 hi + int16 lo) with double-float SpMV on fp32 pipes; double-float (fp32 pair) CG vectors, f64 dot finish and reliable updates",
+        "dtype": "f64 residual / VJP assembly, double-float (fp32 pair) matrix assembly; DF48 matrix (fp32 hi + int16 lo) with double-float SpMV on fp32 pipes; double-float CG vectors, f64 dot finish and reliable updates",
         "data": "synthetic",
         "config": {"workload": name, "precision": args.precision, "tolerance": RTOL,
                    "solver": "block-Jacobi PCG, DF48 SpMV + double-float CG vectors, FP64 reliable updates (true residual)",
                    "l2": "inputs larger than L2 (the DF48 matrix alone is 1.5 GB > 129 MB)",
                    "replicas": "one independent problem per GPU (no data-path collective)"},
         "pcg_iterations": its_mx,
+        "throughput": {"cells_per_s": cells * world / value, "dofs_per_s": nodes * 3 * world / value,
+                       "cg_iterations_per_s": sum(its_mx) / max(args.steps, 1) * world / value,
+                       "note": "one TO iteration (assemble + forward solve + adjoint + gradient) per unit of value"},
         "phases_s": {k: v / args.steps for k, v in phases_mx.items()},
         "fp64": fp64,
         "e2e": {"value": t_e2e / args.steps / world, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -866,6 +920,7 @@ def main():
                      "sliced_df48": roof.get("df48") if head != "df48" else None},
         "cpu_baseline": cpu,
         "clocks": clocks,
+        "assembly": asm_roof,
         "gpu_launches": int(launches),
     }
     if rank == 0:

@@ -104,6 +104,13 @@ typedef struct fem_mesh_t {
   int64_t n_cells;
   const double* coords;     /* (n_nodes, 3)                                       */
   const int32_t* conn;      /* (n_cells, nodes_per_cell), meshio node order       */
+  /* Optional per-cell geometry from fem_cell_geometry (both or neither): the
+   * (n_cells, nq, nodes_per_cell, 3) physical shape gradients and (n_cells, nq) JxW.
+   * When set, the cell kernels read them instead of recomputing the Jacobians;
+   * NULL: recomputed in every launch.  Replaces nothing: the reference keeps the
+   * same arrays (problem.py:130-147, fe.shape_grads / fe.JxW). */
+  const double* shape_grads;
+  const double* jxw;
 } fem_mesh_t;
 
 typedef struct fem_pattern_t {
@@ -205,6 +212,11 @@ int fem_pattern_scalar(int64_t n_nodes, int32_t vec, const int64_t* block_ptr, c
  * kernels jax_fem/problem.py:216-259. */
 int fem_quad_points(const fem_mesh_t* mesh, double* x_out /* (n_cells,nq,3) */,
                     double* jxw_out /* (n_cells,nq) or NULL */, void* stream);
+/* Physical shape gradients (n_cells, nq, nodes_per_cell, 3) and JxW (n_cells, nq) in FP64
+ * (fe.py:112-141 get_shape_grads, kept by problem.py:130-147 initialize_geometric_quantities):
+ * J = sum_a (x_a - x_0) (x) dN_a/dxi, grads = dN/dxi J^-1, JxW = det J w_q.  Store the two
+ * pointers in fem_mesh_t.shape_grads / .jxw to let the cell kernels reuse them. */
+int fem_cell_geometry(const fem_mesh_t* mesh, double* shape_grads, double* jxw, void* stream);
 int fem_face_quad_points(const fem_mesh_t* mesh, const int32_t* face_cells, const int32_t* face_ids,
                          int64_t n_faces, double* x_out /* (n_faces,nfq,3) */,
                          double* nanson_out /* (n_faces,nfq) or NULL */, void* stream);
@@ -230,7 +242,11 @@ int fem_surface_robin(const fem_mesh_t* mesh, const fem_pattern_t* pat, const in
  * compute_residual_vars_helper :426-437, compute_newton_vars :447-460 and the
  * PETSc setValuesCOO/assemble jax_fem/solver.py:522-526.
  * outputs: FEM_OUT_RESIDUAL  residual += R_int(u)           (FP64 always)
- *          FEM_OUT_MATRIX    vals += K(u) in `precision`    (consistent hand-derived tangent)
+ *          FEM_OUT_MATRIX    vals += K(u) in `precision`    (consistent hand-derived tangent;
+ *                            FEM_F32 / FEM_F64 values; FEM_DF48: FP64 values computed in
+ *                            double-float arithmetic on the FP32 pipes, ~2^-46 relative, for
+ *                            the DF48 solver copies -- isotropic materials (linear elastic,
+ *                            SIMP) with the mesh's geometry cache; others assemble in FP64)
  *          FEM_OUT_APPLY     apply_out += K(u) w            (FP64 always)
  * Outputs are accumulated (the caller zeroes them).  bc_mode controls which
  * matrix entries are skipped (FEM_BC_*); bc_mask is one byte per dof.  With a

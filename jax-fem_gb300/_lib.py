@@ -34,7 +34,7 @@ class FemError(RuntimeError):
 
 class FemMesh(C.Structure):
     _fields_ = [("elem_type", C.c_int32), ("vec", C.c_int32), ("n_nodes", C.c_int64), ("n_cells", C.c_int64),
-                ("coords", C.c_void_p), ("conn", C.c_void_p)]
+                ("coords", C.c_void_p), ("conn", C.c_void_p), ("shape_grads", C.c_void_p), ("jxw", C.c_void_p)]
 
 
 class FemPattern(C.Structure):
@@ -79,6 +79,7 @@ SIGNATURES = {
     "fem_pattern_slots": ([I32, P, I64, P, P, P, P], C.c_int),
     "fem_pattern_scalar": ([I64, I32, P, P, P, P, P, P], C.c_int),
     "fem_quad_points": ([PMESH, P, P, P], C.c_int),
+    "fem_cell_geometry": ([PMESH, P, P, P], C.c_int),
     "fem_face_quad_points": ([PMESH, P, P, I64, P, P, P], C.c_int),
     "fem_body_load": ([PMESH, P, P, P], C.c_int),
     "fem_surface_load": ([PMESH, P, P, I64, P, P, P], C.c_int),

@@ -30,6 +30,9 @@ static int fill_params(const fem_mesh_t* mesh, const fem_material_t* mat, AsmPar
   P.tab = make_vol_tables(mesh->elem_type);
   P.coords = mesh->coords;
   P.conn = mesh->conn;
+  FEM_REQUIRE((mesh->shape_grads == nullptr) == (mesh->jxw == nullptr), "set both or neither of shape_grads / jxw");
+  P.grads = mesh->shape_grads;
+  P.jxw = mesh->jxw;
   P.n_cells = mesh->n_cells;
   if (mat) {
     FEM_REQUIRE(mat->n_consts >= 0 && mat->n_consts <= 96, "n_consts must be in [0, 96]");
@@ -233,6 +236,54 @@ extern "C" int fem_quad_points(const fem_mesh_t* mesh, double* x_out, double* jx
   return check_launch("quad_points_kernel");
 }
 
+// Cached per-cell geometry: thread per (cell, quadrature point), the cell kernels' own
+// arithmetic (qp_geometry on cell-local coordinates) in FP64.
+template <int NN, int NQ>
+__global__ void cell_geometry_kernel(VolTables tab, const double* coords, const int32_t* conn, int64_t n_cells,
+                                     double* grads, double* jxw) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_cells * NQ;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = k / NQ;
+    const int q = (int)(k % NQ);
+    double X[NN * 3], dN[NN * 3];
+    const int n0 = conn[e * NN];
+    for (int n = 0; n < NN; ++n) {
+      const int node = conn[e * NN + n];
+      for (int d = 0; d < 3; ++d) {
+        X[n * 3 + d] = coords[(int64_t)node * 3 + d] - coords[(int64_t)n0 * 3 + d];
+        dN[n * 3 + d] = tab.dN[q][n][d];
+      }
+    }
+    double w;
+    qp_geometry<NN, double>(X, dN, tab.w[q], grads + k * (NN * 3), w);
+    jxw[k] = w;
+  }
+}
+
+extern "C" int fem_cell_geometry(const fem_mesh_t* mesh, double* shape_grads, double* jxw, void* stream) {
+  int rc = check_mesh(mesh);
+  if (rc) return rc;
+  FEM_REQUIRE(shape_grads && jxw, "NULL output");
+  if (mesh->n_cells == 0) return FEM_OK;
+  VolTables tab = make_vol_tables(mesh->elem_type);
+  const int64_t work = mesh->n_cells * tab.nq;
+  cudaStream_t s = as_stream(stream);
+  const int g = grid_for(work, 128);
+  switch (mesh->elem_type) {
+    case FEM_HEX8:
+      cell_geometry_kernel<8, 8><<<g, 128, 0, s>>>(tab, mesh->coords, mesh->conn, mesh->n_cells, shape_grads, jxw);
+      break;
+    case FEM_TET10:
+      cell_geometry_kernel<10, 4><<<g, 128, 0, s>>>(tab, mesh->coords, mesh->conn, mesh->n_cells, shape_grads, jxw);
+      break;
+    default:
+      cell_geometry_kernel<4, 1><<<g, 128, 0, s>>>(tab, mesh->coords, mesh->conn, mesh->n_cells, shape_grads, jxw);
+      break;
+  }
+  note_launches(1);
+  return check_launch("cell_geometry_kernel");
+}
+
 extern "C" int fem_face_quad_points(const fem_mesh_t* mesh, const int32_t* face_cells, const int32_t* face_ids,
                                     int64_t n_faces, double* x_out, double* nanson_out, void* stream) {
   int rc = check_mesh(mesh);
@@ -284,7 +335,8 @@ extern "C" int fem_assemble(const fem_mesh_t* mesh, const fem_material_t* mat, c
   if (rc) return rc;
   FEM_REQUIRE(mat != nullptr, "material NULL");
   FEM_REQUIRE((outputs & ~7) == 0 && outputs != 0, "outputs must be a non-empty FEM_OUT_* mask");
-  FEM_REQUIRE(precision == FEM_F32 || precision == FEM_F64, "precision must be FEM_F32 or FEM_F64");
+  FEM_REQUIRE(precision == FEM_F32 || precision == FEM_F64 || precision == FEM_DF48,
+              "precision must be FEM_F32, FEM_F64 or FEM_DF48");
   FEM_REQUIRE(bc_mode >= FEM_BC_NONE && bc_mode <= FEM_BC_SYMMETRIC, "bad bc_mode");
   FEM_REQUIRE(bc_mode == FEM_BC_NONE || bc_mask, "bc_mode needs bc_mask");
   if (outputs & FEM_OUT_RESIDUAL) FEM_REQUIRE(residual && u, "residual output needs u and residual");
@@ -309,11 +361,11 @@ extern "C" int fem_assemble(const fem_mesh_t* mesh, const fem_material_t* mat, c
     P.slots = pat->slots;
   }
   cudaStream_t s = as_stream(stream);
-  if (precision == FEM_F32 && (outputs & FEM_OUT_MATRIX)) {
-    // FP32 matrix, FP64 residual / tangent action in a separate pass
+  if ((precision == FEM_F32 || precision == FEM_DF48) && (outputs & FEM_OUT_MATRIX)) {
+    // FP32 / double-float matrix, FP64 residual / tangent action in a separate pass
     AsmParams Pm = P;
     Pm.outputs = FEM_OUT_MATRIX;
-    rc = run_cell_kernel(mesh, Pm, mat->kind, FEM_F32, KMODE_ASSEMBLE, s);
+    rc = run_cell_kernel(mesh, Pm, mat->kind, precision, KMODE_ASSEMBLE, s);
     if (rc) return rc;
     const int rest = outputs & ~FEM_OUT_MATRIX;
     if (!rest) return FEM_OK;

@@ -18,6 +18,7 @@
 #pragma once
 
 #include "fem_common.cuh"
+#include "fem_df.cuh"
 #include "fem_elements.cuh"
 #include "fem_materials.cuh"
 
@@ -28,6 +29,8 @@ struct AsmParams {
   MatConsts mc;
   const double* coords;
   const int32_t* conn;
+  const double* grads;    // optional cached (n_cells, NQ, NN, 3) physical shape gradients
+  const double* jxw;      // and (n_cells, NQ) JxW (fem_cell_geometry); NULL: recomputed
   int64_t n_cells;
   const double* u;
   const double* w;
@@ -73,6 +76,28 @@ struct AsmLayout {
   static constexpr size_t bytes = sizeof(T) * (size_t)nT + sizeof(int) * CPB * NN + sizeof(double) * THREADS + 16;
 };
 
+// Geometry at one quadrature point from cell-local node coordinates X (x_a - x_0, NN x 3) and the
+// reference gradients dN (NN x 3) at that point: J = sum_a X_a (x) dN_a, physical gradients
+// G_a = dN_a J^-1 (NN x 3), JxW = det J w.  One routine for the cell kernels and for the cached
+// geometry (fem_cell_geometry), so both give the same bits.
+template <int NN, typename T>
+__device__ __forceinline__ void qp_geometry(const T* X, const T* dN, T w, T* G, T& jxw) {
+  T J[3][3] = {};
+  for (int n = 0; n < NN; ++n)
+    for (int d = 0; d < 3; ++d) {
+      const T x = X[n * 3 + d];
+      for (int r = 0; r < 3; ++r) J[d][r] += x * dN[n * 3 + r];
+    }
+  const T det = det3<T>(J);
+  T Ji[3][3];
+  inv3<T>(J, det, Ji);
+  jxw = det * w;
+  for (int n = 0; n < NN; ++n) {
+    const T* dn = dN + n * 3;
+    for (int d = 0; d < 3; ++d) G[n * 3 + d] = dn[0] * Ji[0][d] + dn[1] * Ji[1][d] + dn[2] * Ji[2][d];
+  }
+}
+
 template <int NN, int NQ, int VEC, int MAT, typename T, int KMODE>
 __global__ void __launch_bounds__(AsmLayout<NN, NQ, VEC, MAT, T>::THREADS)
 cell_kernel(const AsmParams P) {
@@ -101,6 +126,7 @@ cell_kernel(const AsmParams P) {
     for (int d = 0; d < 3; ++d) sdN[k * 3 + d] = T(P.tab.dN[q][n][d]);
   }
 
+  const bool cached = P.grads != nullptr;   // geometry from fem_cell_geometry
   const bool want_res = (KMODE == KMODE_ASSEMBLE) && (P.outputs & FEM_OUT_RESIDUAL);
   const bool want_mat = (KMODE == KMODE_ASSEMBLE) && (P.outputs & FEM_OUT_MATRIX);
   const bool want_app = (KMODE == KMODE_ASSEMBLE) && (P.outputs & FEM_OUT_APPLY);
@@ -119,8 +145,11 @@ cell_kernel(const AsmParams P) {
       if (e < P.n_cells) node = P.conn[e * NN + n];
       sConn[k] = node;
       if (node >= 0) {
-        const int n0 = P.conn[e * NN];
-        for (int d = 0; d < 3; ++d) sX[k * 3 + d] = T(P.coords[(int64_t)node * 3 + d] - P.coords[(int64_t)n0 * 3 + d]);
+        if (!cached) {
+          const int n0 = P.conn[e * NN];
+          for (int d = 0; d < 3; ++d)
+            sX[k * 3 + d] = T(P.coords[(int64_t)node * 3 + d] - P.coords[(int64_t)n0 * 3 + d]);
+        }
         for (int v = 0; v < VEC; ++v) {
           const int64_t dof = (int64_t)node * VEC + v;
           sU[k * VEC + v] = P.u ? T(P.u[dof]) : T(0);
@@ -137,32 +166,27 @@ cell_kernel(const AsmParams P) {
         for (int v = 0; v < VEC; ++v) { sU[k * VEC + v] = T(0); if (need_w) sW[k * VEC + v] = T(0); }
       }
     }
+    if (cached) {   // the tile's cached shape gradients, one contiguous run
+      constexpr int GT = CPB * NQ * NN * 3;
+      const int64_t avail = (P.n_cells - tile * CPB) * (NQ * NN * 3);
+      const double* src = P.grads + tile * (int64_t)GT;
+      for (int k = tid; k < GT; k += blockDim.x) sG[k] = k < avail ? T(src[k]) : T(0);
+    }
     __syncthreads();
     // ---- B: geometry + material at quadrature points ----------------------
     for (int k = tid; k < CPB * NQ; k += blockDim.x) {
       const int c = k / NQ, q = k % NQ;
       const int64_t e = tile * CPB + c;
       if (e >= P.n_cells) continue;
-      const T* X = sX + c * NN * 3;
-      T J[3][3] = {};
-      for (int n = 0; n < NN; ++n)
-        for (int d = 0; d < 3; ++d) {
-          const T x = X[n * 3 + d];
-          for (int r = 0; r < 3; ++r) J[d][r] += x * sdN[(q * NN + n) * 3 + r];
-        }
-      const T det = det3<T>(J);
-      T Ji[3][3];
-      inv3<T>(J, det, Ji);
-      const T jxw = det * T(P.tab.w[q]);
       T* G = sG + (c * NQ + q) * NN * 3;
+      T jxw;
+      if (cached) jxw = T(P.jxw[e * NQ + q]);
+      else qp_geometry<NN, T>(sX + c * NN * 3, sdN + q * NN * 3, T(P.tab.w[q]), G, jxw);
       T gu[NS];
       T gw[NS];
       for (int s = 0; s < NS; ++s) { gu[s] = T(0); gw[s] = T(0); }
       for (int n = 0; n < NN; ++n) {
-        const T* dn = sdN + (q * NN + n) * 3;
-        T g[3];
-        for (int d = 0; d < 3; ++d) g[d] = dn[0] * Ji[0][d] + dn[1] * Ji[1][d] + dn[2] * Ji[2][d];
-        for (int d = 0; d < 3; ++d) G[n * 3 + d] = g[d];
+        const T g[3] = {G[n * 3], G[n * 3 + 1], G[n * 3 + 2]};
         for (int v = 0; v < VEC; ++v) {
           const T un = sU[(c * NN + n) * VEC + v];
           for (int d = 0; d < 3; ++d) gu[v * 3 + d] += un * g[d];
@@ -385,6 +409,147 @@ cell_kernel(const AsmParams P) {
   }
 }
 
+// ---- isotropic tangent in double-float (FEM_DF48 matrix assembly) ----------------------------
+// The matrix of the linear isotropic laws (linear elastic, SIMP) for the DF48 solver copies, with
+// the node-pair form of cell_kernel (K_ab = cr M_ab + M_ab^T + tr(M_ab) I, M_ab = sum_q mu_q JxW_q
+// g_qa (x) g_qb, cr = lam / mu the same at every point) evaluated in double-float arithmetic on
+// the FP32 pipes: GB300's FP64 pipe (~1/64 of FP32) bounds the FP64 form.  Reads the cached
+// geometry (fem_cell_geometry).  Per tile of CPB cells:
+//   1  mu_q JxW_q per (cell, qp) in FP64 (the material law, a few flops) and the connectivity;
+//   2  the cell's shape gradients and mu JxW g as double-float pairs in shared memory (FP64 ->
+//      pair from the bits: integer operations);
+//   3  one thread per (cell, node pair a <= b): 9 double-float product-accumulates per qp, then
+//      K_ab, each value rounded once to FP64 (one FP64 add) and scattered with FP64 atomics
+//      into block (a, b) and, for a != b, its transpose (Dirichlet rules of cell_kernel).
+// The values carry ~2^-46 relative rounding against FP64's 2^-53: far below the 2^-40 of the DF48
+// copy made from them.
+constexpr int DFM_THREADS = 288;
+template <int NN>
+struct DfmLayout {
+  static constexpr int NP = NN * (NN + 1) / 2;
+  static constexpr int CPB = DFM_THREADS / NP > 0 ? DFM_THREADS / NP : 1;
+};
+
+template <int NN, int NQ, int MAT>
+__global__ void __launch_bounds__(DFM_THREADS, 4) cell_matrix_df_kernel(const AsmParams P) {
+  using Mat = Material<MAT, 3, double>;
+  constexpr int NP = DfmLayout<NN>::NP, CPB = DfmLayout<NN>::CPB, GQ = NN * 3;
+  __shared__ float2 sg[CPB * NQ * GQ];   // g_qa (double-float)
+  __shared__ float2 sm[CPB * NQ * GQ];   // mu_q JxW_q g_qa (double-float)
+  __shared__ float2 smu[CPB * NQ];       // mu_q JxW_q (double-float)
+  __shared__ int sconn[CPB * NN];
+  const int tid = threadIdx.x;
+  const df2 cr = df_from_bits(Mat::lam_over_mu(P.mc));
+  double* vals = reinterpret_cast<double*>(P.vals);
+  const int64_t n_tiles = (P.n_cells + CPB - 1) / CPB;
+  for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    __syncthreads();
+    for (int k = tid; k < CPB * NQ; k += blockDim.x) {
+      const int64_t e = tile * CPB + k / NQ;
+      double smq = 0.0;
+      if (e < P.n_cells) {
+        const int q = k % NQ;
+        const double* qp = P.qp_params ? P.qp_params + (e * NQ + q) * P.n_qp : nullptr;
+        const double g0[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        double S[9], tan[2];
+        Mat::eval(g0, P.mc, qp, nullptr, S, tan, true);
+        smq = tan[1] * P.jxw[e * NQ + q];
+      }
+      const df2 sd = df_from_bits(smq);
+      smu[k] = make_float2(sd.h, sd.l);
+    }
+    for (int k = tid; k < CPB * NN; k += blockDim.x) {
+      const int64_t e = tile * CPB + k / NN;
+      sconn[k] = e < P.n_cells ? P.conn[e * NN + k % NN] : -1;
+    }
+    __syncthreads();
+    {
+      constexpr int GT = CPB * NQ * GQ;
+      const int64_t avail = (P.n_cells - tile * CPB) * (NQ * GQ);
+      const double* src = P.grads + tile * (int64_t)GT;
+      for (int k = tid; k < GT; k += blockDim.x) {
+        const double g = k < avail ? src[k] : 0.0;
+        const df2 gd = df_from_bits(g);
+        const float2 mu = smu[k / GQ];
+        const df2 md = df_mul(df2{mu.x, mu.y}, gd);
+        sg[k] = make_float2(gd.h, gd.l);
+        sm[k] = make_float2(md.h, md.l);
+      }
+    }
+    __syncthreads();
+    for (int t = tid; t < CPB * NP; t += blockDim.x) {
+      const int cc = t / NP;
+      int pp = t - cc * NP, pa = 0;
+      while (pp >= NN - pa) { pp -= NN - pa; ++pa; }
+      const int pb = pa + pp;
+      const int64_t ee = tile * CPB + cc;
+      if (ee >= P.n_cells) continue;
+      float mh[9], ml[9];
+#pragma unroll
+      for (int v = 0; v < 9; ++v) { mh[v] = 0.f; ml[v] = 0.f; }
+#pragma unroll 2
+      for (int q = 0; q < NQ; ++q) {
+        const float2* ma = sm + (cc * NQ + q) * GQ + pa * 3;
+        const float2* gb = sg + (cc * NQ + q) * GQ + pb * 3;
+        const float2 m0 = ma[0], m1 = ma[1], m2 = ma[2], g0 = gb[0], g1 = gb[1], g2 = gb[2];
+        const df2 m[3] = {df2{m0.x, m0.y}, df2{m1.x, m1.y}, df2{m2.x, m2.y}};
+        const df2 g[3] = {df2{g0.x, g0.y}, df2{g1.x, g1.y}, df2{g2.x, g2.y}};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) df_acc(mh[i * 3 + j], ml[i * 3 + j], m[i], g[j]);
+      }
+      df2 M[9];
+#pragma unroll
+      for (int v = 0; v < 9; ++v) M[v] = df_fast(mh[v], ml[v]);
+      const df2 tr = df_add(df_add(M[0], M[4]), M[8]);
+      const int64_t na2 = sconn[cc * NN + pa], nb2 = sconn[cc * NN + pb];
+      const int sab = P.slots[(ee * NN + pa) * NN + pb], sba = P.slots[(ee * NN + pb) * NN + pa];
+      // row pointers and Dirichlet flags of the pair's six rows, read once (byte pointers may
+      // alias the values, so they would be re-read after every atomic otherwise)
+      double* dst_a[3];
+      double* dst_b[3];
+      bool abc[3], bbc[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        dst_a[r] = vals + P.indptr[na2 * 3 + r] + 3 * sab;
+        dst_b[r] = vals + P.indptr[nb2 * 3 + r] + 3 * sba;
+        abc[r] = P.bc && P.bc[na2 * 3 + r];
+        bbc[r] = P.bc && P.bc[nb2 * 3 + r];
+      }
+      const bool keep_rows = P.bc_mode == FEM_BC_NONE, sym = P.bc_mode == FEM_BC_SYMMETRIC;
+#pragma unroll
+      for (int ii = 0; ii < 3; ++ii) {
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk) {
+          df2 kv = df_add(df_mul(cr, M[ii * 3 + kk]), M[kk * 3 + ii]);   // K_ab[ii][kk]
+          if (ii == kk) kv = df_add(kv, tr);
+          const double kd = f2d_bits(kv.h) + f2d_bits(kv.l);
+          // K[(a,ii),(b,kk)]: row of a, column of b; K[(b,kk),(a,ii)]: its transpose
+          if (!(abc[ii] && !keep_rows) && !(bbc[kk] && sym)) atomicAdd(dst_a[ii] + kk, kd);
+          if (pa != pb && !(bbc[kk] && !keep_rows) && !(abc[ii] && sym)) atomicAdd(dst_b[kk] + ii, kd);
+        }
+      }
+    }
+  }
+}
+
+template <int NN, int NQ, int MAT>
+int launch_cell_matrix_df(const AsmParams& P, cudaStream_t stream) {
+  using L = DfmLayout<NN>;
+  auto kern = cell_matrix_df_kernel<NN, NQ, MAT>;
+  const int64_t tiles = (P.n_cells + L::CPB - 1) / L::CPB;
+  int blocks_per_sm = 1;
+  FEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, DFM_THREADS, 0));
+  if (blocks_per_sm < 1) blocks_per_sm = 1;
+  int64_t grid = (int64_t)sm_count() * blocks_per_sm;
+  if (grid > tiles) grid = tiles;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, DFM_THREADS, 0, stream>>>(P);
+  note_launches(1);
+  return check_launch("cell_matrix_df_kernel");
+}
+
 // Host-side launcher for one (element, vec, material, precision, mode).
 template <int NN, int NQ, int VEC, int MAT, typename T, int KMODE>
 int launch_cell_kernel(const AsmParams& P, cudaStream_t stream) {
@@ -413,6 +578,11 @@ int dispatch_precision(const AsmParams& P, int precision, int kmode, cudaStream_
     return fail(FEM_ERR_UNSUPPORTED, "history VJP is defined for J2 only");
   }
   if (precision == FEM_F32) return launch_cell_kernel<NN, NQ, VEC, MAT, float, KMODE_ASSEMBLE>(P, s);
+  if (precision == FEM_DF48) {
+    // double-float matrix for the isotropic laws with cached geometry; FP64 otherwise
+    if constexpr (VEC == 3 && MatTraits<MAT, VEC>::TAN == TAN_ISO)
+      if (P.grads && P.outputs == FEM_OUT_MATRIX) return launch_cell_matrix_df<NN, NQ, MAT>(P, s);
+  }
   return launch_cell_kernel<NN, NQ, VEC, MAT, double, KMODE_ASSEMBLE>(P, s);
 }
 

@@ -19,6 +19,7 @@
 #include <mutex>
 
 #include "fem_common.cuh"
+#include "fem_df.cuh"
 #include "fem_elements.cuh"
 
 namespace fem {
@@ -212,90 +213,10 @@ __device__ __forceinline__ void reduce_and_finalize(double (&v)[3], KCtl* C, int
 enum { FMT_F32 = 0, FMT_F64 = 1, FMT_DF = 2 };
 constexpr int SPMV_G = 8;
 
-__device__ __forceinline__ float df_lo_scale(float hi) {
-  const int e = (__float_as_int(hi) >> 23) & 0xFF;
-  return e > 39 ? __int_as_float((e - 39) << 23) : 0.0f;   // 2^(e - 166) = ulp(hi) / 2^16
-}
-
-// DF48 correction without an int->float conversion: base is the float 1.5 * 2^(E-143) (E the
-// exponent field of hi); adding q (|q| < 2^15) to its mantissa field gives (1.5 + q/2^23) *
-// 2^(E-143), and subtracting base leaves exactly q * 2^(E-166) = q * ulp(hi) / 2^16.  Encoders
-// write q = 0 whenever E <= 39, where base may wrap: the result is then 0 as required.
-__device__ __forceinline__ float df48_lo(float hi, int q) {
-  const int base = (__float_as_int(hi) & 0x7f800000) + (0x400000 - (16 << 23));
-  return __int_as_float(base + q) - __int_as_float(base);
-}
-
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& err) {
-  s = a + b;
-  const float bb = s - a;
-  err = (a - (s - bb)) + (b - bb);
-}
-
-// ---- double-float CG recurrence (all vector arithmetic on FP32 pipes) ----------------
-// A df value is an unevaluated float pair h + l with |l| <= ulp(h)/2 (~48-bit mantissa).
-// GB300's FP64 pipe is ~1/64 of its FP32 rate, so the mixed solver keeps x, r, p, q in this
-// form and touches FP64 only to finish per-thread dot partials and in the scalar recurrences.
-struct df2 { float h, l; };
-
-__device__ __forceinline__ df2 df_fast(float s, float e) {  // |s| >= |e|
-  const float h = s + e;
-  return df2{h, e - (h - s)};
-}
-__device__ __forceinline__ df2 df_add(df2 a, df2 b) {
-  float s, e;
-  two_sum(a.h, b.h, s, e);
-  e += a.l + b.l;
-  return df_fast(s, e);
-}
-__device__ __forceinline__ df2 df_mul(df2 a, df2 b) {
-  const float p = a.h * b.h;
-  float e = fmaf(a.h, b.h, -p);
-  e = fmaf(a.h, b.l, e);
-  e = fmaf(a.l, b.h, e);
-  return df_fast(p, e);
-}
-__device__ __forceinline__ df2 df_of(double d) {
-  const float h = __double2float_rn(d);
-  return df2{h, __double2float_rn(d - (double)h)};
-}
-__device__ __forceinline__ double df_dbl(df2 a) { return (double)a.h + (double)a.l; }
-
-// An FP64 value as a double-float pair built from its bits with integer and FP32 operations only
-// (GB300's FP64 pipe runs ~1/64 of the FP32 rate): h keeps the sign, the exponent and the leading
-// 24 significand bits, l the next 29 bits (rounded to 24), renormalised.  For |v| inside FP32's
-// normal range; the CG's vectors are range-scaled to an RMS near 1.  Values whose l would fall
-// below FP32's normal range keep h only (|v| below ~2^-74: far under the vectors' rounding).
-__device__ __forceinline__ df2 df_from_bits(double v) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
-  const int e = (int)((hw >> 20) & 0x7FFu) - 1023;          // unbiased exponent
-  const unsigned sgn = hw & 0x80000000u;
-  if (e < -126) return df2{0.f, 0.f};
-  if (e > 127) return df2{__int_as_float(sgn | 0x7F800000u), 0.f};
-  const float h = __int_as_float(sgn | ((unsigned)(e + 127) << 23) | ((hw & 0xFFFFFu) << 3) | (lw >> 29));
-  float l = 0.f;
-  if (e - 52 >= -126) l = __int_as_float(sgn | 0x3F800000u) * (float)(lw & 0x1FFFFFFFu) *
-                          __int_as_float((unsigned)(e - 52 + 127) << 23);
-  return df_fast(h, l);
-}
-
 // Component stride of the FP64 transposed-part vector qT of the symmetric SpMVs (component c of
 // node i at c * qt_stride + i): the node count rounded up to 32, so that each component of a
 // 32-node tile is one 256-byte run (a bulk copy needs 16-byte aligned runs).
 __host__ __device__ __forceinline__ int64_t qt_stride(int64_t n_nodes) { return (n_nodes + 31) & ~int64_t(31); }
-// accumulate a*b into (sh, sl) without renormalising every step
-__device__ __forceinline__ void df_acc(float& sh, float& sl, df2 a, df2 b) {
-  const float p = a.h * b.h;
-  float e = fmaf(a.h, b.h, -p);
-  e = fmaf(a.h, b.l, e);
-  e = fmaf(a.l, b.h, e);
-  float t, te;
-  two_sum(sh, p, t, te);
-  sl += te + e;
-  sh = t;
-}
-
 // Double-float form of reduce_and_finalize for the double-float kernels: per-thread pairs are
 // summed in double-float on the FP32 pipes (shuffles within a warp, then one warp over the warps'
 // sums), each CTA stores its pairs as floats in its partials slot, and the last CTA sums the slots

@@ -144,18 +144,6 @@ __device__ __forceinline__ void df3_add(float* dh, float* dl, const float* h, co
   }
 }
 
-// FP32 -> FP64 from the bits (integer operations; GB300's FP64 pipe is ~1/64 of the FP32 rate):
-// exact for normal floats, FP32 subnormals become 0.
-__device__ __forceinline__ double f2d_bits(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xFFu;
-  if (e == 0u) return 0.0;
-  unsigned long long d = ((unsigned long long)(b & 0x80000000u) << 32) |
-                         ((unsigned long long)(e == 255u ? 2047u : e + 896u) << 52) |
-                         ((unsigned long long)(b & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)d);
-}
-
 // qT[c][node] += h + l (component stride qt_stride).  For emissions made by every lane of a warp:
 // one FP64 add per nonzero component (a warp-wide FP64 instruction serves 32 rows).
 __device__ __forceinline__ void ss_atomic3(double* qT, int64_t stride, int64_t node, const float* h, const float* l) {

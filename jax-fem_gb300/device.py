@@ -201,7 +201,8 @@ class Engine:
         self.coords = torch.as_tensor(fe.points, dtype=torch.float64, device=dev).contiguous()
         self.conn = torch.as_tensor(fe.cells, dtype=torch.int32, device=dev).contiguous()
         self.mesh = _lib.FemMesh(fe.elem_id, self.vec, self.num_nodes, self.num_cells,
-                                 self.coords.data_ptr(), self.conn.data_ptr())
+                                 self.coords.data_ptr(), self.conn.data_ptr(), None, None)
+        self._build_geometry()
         self._build_pattern()
         self._bc_seen = None
         self.bc_value_terms = []
@@ -216,6 +217,23 @@ class Engine:
         self._robin = []            # (face_cells, face_ids, degree, coeffs) of u-dependent surface maps
         self._uk = None             # compiled universal kernels (get_universal_kernel[s_surface])
         self._uk_key = None
+
+    def _build_geometry(self):
+        """Physical shape gradients and JxW of every cell and quadrature point, computed once on the
+        device and kept, as the reference keeps fe.shape_grads / fe.JxW (problem.py:130-147); the
+        cell kernels then read them instead of recomputing the Jacobians on the FP64 pipe.  Kept
+        only while it takes at most a quarter of the free device memory (1.6 GB per 1M HEX8 cells);
+        otherwise the kernels recompute the geometry."""
+        self.shape_grads = self.jxw = None
+        n = self.num_cells * self.num_quads
+        need = n * (self.nn * 3 + 1) * 8
+        if n == 0 or need > torch.cuda.mem_get_info(self.device)[0] // 4:
+            return
+        self.shape_grads = torch.empty(n * self.nn * 3, dtype=torch.float64, device=self.device)
+        self.jxw = torch.empty(n, dtype=torch.float64, device=self.device)
+        call("fem_cell_geometry", C.byref(self.mesh), ptr(self.shape_grads), ptr(self.jxw), _stream())
+        self.mesh.shape_grads = self.shape_grads.data_ptr()
+        self.mesh.jxw = self.jxw.data_ptr()
 
     def add_robin(self, boundary_inds, coeffs):
         """Register the u-dependent polynomial part of a surface map on the faces boundary_inds."""
@@ -431,19 +449,24 @@ class Engine:
                      _stream())
         return res
 
-    def tangent(self, dofs, precision, bc_mode, cache=True):
+    def tangent(self, dofs, precision, bc_mode, cache=True, df_source=False):
         """Assemble K(u) in `precision` with Dirichlet handling `bc_mode` and unit BC diagonal.
-        FEM_DF48 matrices are assembled in FP64 and split into the 6-byte double-float format."""
+        The DF48 solver copies are split from an FP64 CSR tangent that the isotropic laws assemble
+        in double-float arithmetic (fem_assemble with FEM_DF48: FP64 values accurate to ~2^-46,
+        beyond what the 40-bit copy keeps); df_source asks for that FP64 CSR itself.  The FP64
+        path's own tangent (precision FEM_F64) is always assembled in FP64."""
         self.refresh_bc()
         m, ms = self.material()
         if precision == _lib.FEM_SSYM_DF48 and (self.grid is None or bc_mode != _lib.FEM_BC_SYMMETRIC):
             precision = _lib.FEM_SLICED_DF48      # no structured copy for this mesh / elimination
-        key = (precision, bc_mode)
+        df_source = df_source and precision == _lib.FEM_F64
+        key = (precision, bc_mode, "df") if df_source else (precision, bc_mode)
         if cache and m.linear and self.robin_linear and not self.has_universal and key in self._tangent_cache:
             return self._tangent_cache[key]
         if precision not in (_lib.FEM_F32, _lib.FEM_F64):
             # solver copies (DF48, sliced FP32 / FP64 / DF48) are converted from the FP64 CSR tangent
-            A64 = self.tangent(dofs, _lib.FEM_F64, bc_mode, cache=cache)
+            df_copy = precision in (_lib.FEM_DF48, _lib.FEM_SLICED_DF48, _lib.FEM_SYM_DF48, _lib.FEM_SSYM_DF48)
+            A64 = self.tangent(dofs, _lib.FEM_F64, bc_mode, cache=cache, df_source=df_copy)
             nb = C.c_size_t()
             call("fem_matrix_bytes", C.byref(self.pattern), self.vec, precision, C.byref(nb))
             name = f"valsx{precision}_{bc_mode}"
@@ -469,7 +492,7 @@ class Engine:
             self._tangent_cache[key] = A
             return A
         dtype = torch.float32 if precision == _lib.FEM_F32 else torch.float64
-        buf_name = f"vals{precision}_{bc_mode}"
+        buf_name = f"vals{precision}_{bc_mode}" + ("df" if df_source else "")
         vals = getattr(self, buf_name, None)
         if vals is None:
             vals = torch.empty(self.nnz, dtype=dtype, device=self.device)
@@ -477,7 +500,8 @@ class Engine:
         vals.zero_()
         dofs = dofs.contiguous()
         call("fem_assemble", C.byref(self.mesh), C.byref(ms), C.byref(self.pattern), _lib.FEM_OUT_MATRIX,
-             precision, ptr(dofs), None, ptr(self.bc_mask), bc_mode, None, ptr(vals), None, _stream())
+             _lib.FEM_DF48 if df_source else precision, ptr(dofs), None, ptr(self.bc_mask), bc_mode, None,
+             ptr(vals), None, _stream())
         if self._robin:
             self._robin_call(_lib.FEM_OUT_MATRIX, precision, dofs, bc_mode=bc_mode, bc=self.bc_mask, vals=vals)
         if self.has_universal:
