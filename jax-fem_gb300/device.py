@@ -62,6 +62,7 @@ class DeviceCSR:
         self.data = vals
         self.bc_mode = bc_mode
         self.source = source          # FP64 matrix a DF48 matrix was split from
+        self.ref64 = None             # the same FP64 values, sliced (DF48 copies: reliable updates)
         n = eng.num_dofs
         self.shape = (n, n)
         self.nnz = eng.nnz
@@ -489,6 +490,8 @@ class Engine:
             view = buf.view(torch.float64) if precision == _lib.FEM_SLICED_F64 else \
                 buf.view(torch.float32) if precision == _lib.FEM_SLICED_F32 else buf
             A = DeviceCSR(self, precision, view, bc_mode, source=A64)
+            if df_copy and bc_mode == _lib.FEM_BC_SYMMETRIC and self.pattern.n_slices > 0:
+                A.ref64 = self._sliced_reference(A64, bc_mode)
             self._tangent_cache[key] = A
             return A
         dtype = torch.float32 if precision == _lib.FEM_F32 else torch.float64
@@ -516,6 +519,21 @@ class Engine:
         A = DeviceCSR(self, precision, vals, bc_mode)
         self._tangent_cache[key] = A
         return A
+
+    def _sliced_reference(self, A64, bc_mode):
+        """Sliced FP64 copy of A64 (the FP64 CSR a DF48 copy was split from): the operator of the
+        mixed solver's FP64 reliable updates (fem_pcg_refined takes FEM_SLICED_F64), whose SpMV
+        runs ~2.3x faster than the CSR one on the same values."""
+        nb = C.c_size_t()
+        call("fem_matrix_bytes", C.byref(self.pattern), self.vec, _lib.FEM_SLICED_F64, C.byref(nb))
+        name = f"valsref_{bc_mode}"
+        buf = getattr(self, name, None)
+        if buf is None or buf.numel() != nb.value:
+            buf = torch.empty(nb.value, dtype=torch.uint8, device=self.device)
+            setattr(self, name, buf)
+        call("fem_matrix_convert", C.byref(self.pattern), self.num_nodes, self.vec, ptr(A64.data),
+             _lib.FEM_SLICED_F64, ptr(buf), _stream())
+        return DeviceCSR(self, _lib.FEM_SLICED_F64, buf.view(torch.float64), bc_mode, source=A64)
 
     def apply(self, dofs, w, skip_bc_rows=True):
         """K(u) w in FP64, matrix-free (tangent action kernel)."""
@@ -699,6 +717,8 @@ class Engine:
         it, up, rn, st = C.c_int64(), C.c_int64(), C.c_double(), C.c_int32()
         t0 = time.perf_counter()
         ref = A32.source if A32.source is not None and A32.source.bc_mode == _lib.FEM_BC_SYMMETRIC else None
+        if ref is not None and getattr(A32, "ref64", None) is not None:
+            ref = A32.ref64      # the same values in the sliced FP64 layout
         call("fem_pcg_refined", C.byref(self.pattern), self.num_nodes, self.vec, A32.precision, ptr(A32.data),
              pc_kind, ptr(pc),
              C.byref(self.mesh), C.byref(ms), ptr(u_lin.contiguous()), None if ref is None else ptr(ref.data),
