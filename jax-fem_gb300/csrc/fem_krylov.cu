@@ -939,6 +939,14 @@ __global__ void split_vec_kernel(const double* __restrict__ v, int64_t n, float*
 }
 
 // ---- vector kernels (thread per node) ----------------------------------------
+// Preconditioner entries per node: the diagonal (FEM_PC_JACOBI), the full VEC x VEC block-Jacobi
+// inverse (FEM_PC_BJACOBI) or, in the double-float CG, its upper triangle m00 m01 m02 m11 m12 m22
+// (PC_BSYM, vec 3: the inverse of a symmetric block is symmetric, so 6 of 9 floats carry it).
+constexpr int PC_BSYM = 3;   // internal template tag next to FEM_PC_NONE / _JACOBI / _BJACOBI
+__host__ __device__ constexpr int pc_width(int pc) {
+  return pc == FEM_PC_BJACOBI ? 9 : pc == PC_BSYM ? 6 : pc == FEM_PC_JACOBI ? 3 : 0;
+}
+
 template <int VEC, typename T, int PC>
 __device__ __forceinline__ void precond(const T* pc, int64_t i, const T (&r)[VEC], T (&z)[VEC]) {
   if constexpr (PC == FEM_PC_NONE) {
@@ -947,6 +955,12 @@ __device__ __forceinline__ void precond(const T* pc, int64_t i, const T (&r)[VEC
   } else if constexpr (PC == FEM_PC_JACOBI) {
 #pragma unroll
     for (int c = 0; c < VEC; ++c) z[c] = pc[VEC * i + c] * r[c];
+  } else if constexpr (PC == PC_BSYM) {
+    static_assert(VEC == 3, "PC_BSYM is the vec-3 block form");
+    const T* B = pc + 6 * i;
+    z[0] = B[0] * r[0] + B[1] * r[1] + B[2] * r[2];
+    z[1] = B[1] * r[0] + B[3] * r[1] + B[4] * r[2];
+    z[2] = B[2] * r[0] + B[4] * r[1] + B[5] * r[2];
   } else {
     const T* B = pc + (int64_t)VEC * VEC * i;
 #pragma unroll
@@ -1203,13 +1217,41 @@ constexpr int VTILE_WARPS = VTHREADS / 32;
 #ifndef FEM_TILE_MIN_BLOCKS
 #define FEM_TILE_MIN_BLOCKS 6   // 40 registers, 48 resident warps per SM: more loads in flight
 #endif
+// z = M r for one node from its entries e (pc_width(PC) floats)
+template <int PC>
+__device__ __forceinline__ void pc3_apply(const float* e, const float (&rv)[3], float (&zv)[3]) {
+  if constexpr (PC == FEM_PC_BJACOBI) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) zv[c] = e[3 * c] * rv[0] + e[3 * c + 1] * rv[1] + e[3 * c + 2] * rv[2];
+  } else if constexpr (PC == PC_BSYM) {
+    zv[0] = e[0] * rv[0] + e[1] * rv[1] + e[2] * rv[2];
+    zv[1] = e[1] * rv[0] + e[3] * rv[1] + e[4] * rv[2];
+    zv[2] = e[2] * rv[0] + e[4] * rv[1] + e[5] * rv[2];
+  } else if constexpr (PC == FEM_PC_JACOBI) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) zv[c] = e[c] * rv[c];
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) zv[c] = rv[c];
+  }
+}
+
+// Upper triangles of the (symmetric) 3x3 block-Jacobi inverses: 9 floats per node -> 6.
+__global__ void bsym_compact_kernel(int64_t n_nodes, const float* __restrict__ pc9, float* __restrict__ pc6) {
+  GRID_STRIDE_NODES(i, n_nodes) {
+    const float* b = pc9 + 9 * i;
+    float* o = pc6 + 6 * i;
+    o[0] = b[0]; o[1] = b[1]; o[2] = b[2]; o[3] = b[4]; o[4] = b[5]; o[5] = b[8];
+  }
+}
+
 template <int PC, bool SYM = false>
 __global__ void __launch_bounds__(VTHREADS, FEM_TILE_MIN_BLOCKS)
 pcgx_update_tile_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restrict__ xl, float* __restrict__ rh,
                         float* __restrict__ rl, float* __restrict__ z, const float2* __restrict__ pp,
                         const float* __restrict__ qh, const float* __restrict__ ql, const float* __restrict__ pc,
                         KCtl* C, double* partials, int op, double* __restrict__ qT) {
-  constexpr int PCW = PC == FEM_PC_BJACOBI ? 9 : PC == FEM_PC_JACOBI ? 3 : 0;
+  constexpr int PCW = pc_width(PC);
   __shared__ float s_r[VTILE_WARPS][96], s_rl[VTILE_WARPS][96], s_z[VTILE_WARPS][96];
   __shared__ float s_pc[VTILE_WARPS][PCW > 0 ? 32 * PCW : 1];
   if (C->done) return;
@@ -1260,17 +1302,7 @@ pcgx_update_tile_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
     if (lane < nn) {
       float rv[3] = {sr[3 * lane], sr[3 * lane + 1], sr[3 * lane + 2]};
       float zv[3];
-      if constexpr (PC == FEM_PC_BJACOBI) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-          zv[c] = spc[9 * lane + 3 * c] * rv[0] + spc[9 * lane + 3 * c + 1] * rv[1] + spc[9 * lane + 3 * c + 2] * rv[2];
-      } else if constexpr (PC == FEM_PC_JACOBI) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) zv[c] = spc[3 * lane + c] * rv[c];
-      } else {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) zv[c] = rv[c];
-      }
+      pc3_apply<PC>(spc + PCW * lane, rv, zv);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         sz[3 * lane + c] = zv[c];
@@ -1303,7 +1335,7 @@ constexpr int UPD_STAGES = 3;
 
 template <int PC, bool SYM = false>
 struct UpdGeom {
-  static constexpr int PCW = PC == FEM_PC_BJACOBI ? 9 : PC == FEM_PC_JACOBI ? 3 : 0;
+  static constexpr int PCW = pc_width(PC);
   static constexpr uint32_t VB = 96 * 4;        // one dof-ordered float array of a tile
   static constexpr uint32_t PB = 32 * 4 * 8;    // p: 32 nodes x 4 (hi, lo) pairs
   static constexpr uint32_t CB = 32 * PCW * 4;  // preconditioner blocks
@@ -1403,17 +1435,7 @@ pcgx_update_bulk_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
     if (lane < nn) {
       const float rv[3] = {srh[3 * lane], srh[3 * lane + 1], srh[3 * lane + 2]};
       float zv[3];
-      if constexpr (PC == FEM_PC_BJACOBI) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-          zv[c] = spc[9 * lane + 3 * c] * rv[0] + spc[9 * lane + 3 * c + 1] * rv[1] + spc[9 * lane + 3 * c + 2] * rv[2];
-      } else if constexpr (PC == FEM_PC_JACOBI) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) zv[c] = spc[3 * lane + c] * rv[c];
-      } else {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) zv[c] = rv[c];
-      }
+      pc3_apply<PC>(spc + PCW * lane, rv, zv);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         sqh[3 * lane + c] = zv[c];
@@ -2298,10 +2320,22 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
   if (SYM) FEM_CUDA(cudaMemsetAsync(qT, 0, sizeof(double) * (size_t)(VEC * qt_stride(n_nodes)), s));
   KCtl* C = w.ctl;
   const int gv = vec_grid(n), gn = vec_grid(n_nodes);
+  // Block-Jacobi in the sliced mode: the kernels stream the upper triangles of the symmetric
+  // inverse blocks (6 of 9 floats per node, 12 B per node less per iteration), copied once here
+  // into the workspace the sliced mode leaves free; the symmetric modes keep the full blocks.
+  constexpr int PCK = (PC == FEM_PC_BJACOBI && VEC == 3 && !SYM) ? PC_BSYM : PC;
+  const float* pck = pc;
+  if constexpr (PCK == PC_BSYM) {
+    float* p6 = reinterpret_cast<float*>(v);
+    v += al(sizeof(float) * 6 * (size_t)n_nodes);
+    bsym_compact_kernel<<<gn, VTHREADS, 0, s>>>(n_nodes, pc, p6);
+    note_launches(1);
+    pck = p6;
+  }
   // tile kernel: one warp per 32-node tile, grid = resident CTAs (no partial second wave)
   static int tile_per_sm = 0;
   if (tile_per_sm == 0 &&
-      (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tile_per_sm, pcgx_update_tile_kernel<PC, SYM>, VTHREADS, 0) !=
+      (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tile_per_sm, pcgx_update_tile_kernel<PCK, SYM>, VTHREADS, 0) !=
            cudaSuccess ||
        tile_per_sm < 1))
     tile_per_sm = 1;
@@ -2349,7 +2383,7 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
   if (!(h.rr_true <= h.thresh2)) {
     FEM_CUDA(cudaMemcpyAsync(&C->delta2, &delta2, sizeof(double), cudaMemcpyHostToDevice, s));
     FEM_CUDA(cudaMemcpyAsync(&C->check2, &check2, sizeof(double), cudaMemcpyHostToDevice, s));
-    pcgx_start_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, rh, rl, z, pp, pc, 1, C, w.partials);
+    pcgx_start_kernel<VEC, PCK><<<gn, VTHREADS, 0, s>>>(n_nodes, rh, rl, z, pp, pck, 1, C, w.partials);
     note_launches(1);
     int64_t launched = 0;
     while (true) {
@@ -2372,7 +2406,7 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
           if (at_max || h.iter >= maxiter) { final_status = FEM_SOLVE_MAXITER; break; }
           if (h.rr_true < stall_factor(delta) * best_rr) { best_rr = h.rr_true; stalls = 0; }
           else if (++stalls >= 3) { final_status = FEM_SOLVE_STAGNATED; break; }
-          pcgx_start_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, rh, rl, z, pp, pc, 0, C, w.partials);
+          pcgx_start_kernel<VEC, PCK><<<gn, VTHREADS, 0, s>>>(n_nodes, rh, rl, z, pp, pck, 0, C, w.partials);
           pcgx_direction_kernel<VEC><<<gn, VTHREADS, 0, s>>>(n_nodes, z, pp, C);
           note_launches(2);
           continue;
@@ -2397,10 +2431,10 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
         if (rc) return rc;
         if (k == 0) spmv_timer_mark(1, s);
         if constexpr (VEC == 3) {
-          if (!launch_update_bulk<PC, SYM>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C, w.partials,
-                                           FIN_PCGR_UPDATE, s, qT))
-            pcgx_update_tile_kernel<PC, SYM><<<gt, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
-                                                                     w.partials, FIN_PCGR_UPDATE, qT);
+          if (!launch_update_bulk<PCK, SYM>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pck, C, w.partials,
+                                            FIN_PCGR_UPDATE, s, qT))
+            pcgx_update_tile_kernel<PCK, SYM><<<gt, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pck,
+                                                                      C, w.partials, FIN_PCGR_UPDATE, qT);
           pcgx_direction3_kernel<<<gv, VTHREADS, 0, s>>>(n, z, pp, C);
         } else {
           pcgx_update_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
