@@ -561,9 +561,19 @@ spmv_sliced_dfdf_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* __rest
 // cp.async.bulk copies completing on one mbarrier per stage.  Lane 0 issues; every lane waits
 // on the stage's phase.  The HBM stream no longer depends on the per-thread load queue, so a
 // warp keeps BULK_STAGES - 1 chunks in flight while it computes on the third.
-constexpr int BULK_WARPS = 4;      // warps per CTA
-constexpr int BULK_STAGES = 3;     // ring depth per warp
-constexpr int BULK_SLOTS = 2;      // block-column slots per stage
+// Ring geometry (measured best on GB300 at 1M HEX8 cells; overridable for tuning sweeps)
+#ifndef FEM_BULK_WARPS
+#define FEM_BULK_WARPS 4
+#endif
+#ifndef FEM_BULK_STAGES
+#define FEM_BULK_STAGES 3
+#endif
+#ifndef FEM_BULK_SLOTS
+#define FEM_BULK_SLOTS 2
+#endif
+constexpr int BULK_WARPS = FEM_BULK_WARPS;     // warps per CTA
+constexpr int BULK_STAGES = FEM_BULK_STAGES;   // ring depth per warp
+constexpr int BULK_SLOTS = FEM_BULK_SLOTS;     // block-column slots per stage
 constexpr long long BULK_WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz: a wait past this is a fault
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -580,6 +590,21 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
                : "memory");
+}
+// The same copy with an L2 eviction-priority hint (a policy from createpolicy): the SpMV streams the
+// matrix evict-first, so the CG vectors it gathers and writes, and that the next kernels read, keep
+// their L2 lines (the plain-load SpMVs use __ldcs for the same effect).
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ void bulk_load_hint(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                               uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;"
+      ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
+      : "memory");
 }
 __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
@@ -626,7 +651,7 @@ struct BulkGeom {
   static constexpr uint32_t LB = VEC * VEC * 32 * 2;  // correction bytes per slot
   static constexpr uint32_t CB = 32 * 4;              // block-column bytes per slot
   static constexpr uint32_t STAGE = BULK_SLOTS * (VB + LB + CB);
-  static constexpr uint32_t BAR_BYTES = 128;          // BULK_WARPS * BULK_STAGES barriers, padded
+  static constexpr uint32_t BAR_BYTES = (BULK_WARPS * BULK_STAGES * 8 + 127) / 128 * 128;   // barriers, padded
   static constexpr uint32_t SMEM = BAR_BYTES + BULK_WARPS * BULK_STAGES * STAGE;
 };
 
@@ -675,9 +700,10 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
       const uint32_t nb = (uint32_t)cnt;
       async_proxy_fence();
       mbar_expect_tx(bars + stage, nb * (G::VB + G::LB + G::CB));
-      bulk_load(st, vals + pk * VV * 32, nb * G::VB, bars + stage);
-      bulk_load(st + BULK_SLOTS * G::VB, vlo + pk * VV * 32, nb * G::LB, bars + stage);
-      bulk_load(st + BULK_SLOTS * (G::VB + G::LB), scols + pk * 32, nb * G::CB, bars + stage);
+      const uint64_t pol = l2_evict_first_policy();
+      bulk_load_hint(st, vals + pk * VV * 32, nb * G::VB, bars + stage, pol);
+      bulk_load_hint(st + BULK_SLOTS * G::VB, vlo + pk * VV * 32, nb * G::LB, bars + stage, pol);
+      bulk_load_hint(st + BULK_SLOTS * (G::VB + G::LB), scols + pk * 32, nb * G::CB, bars + stage, pol);
     }
     pk += cnt;
     return true;
@@ -1014,6 +1040,9 @@ __global__ void pcg_update_kernel(int64_t n_nodes, T* x, T* r, T* z, const T* p,
 #pragma unroll
     for (int c = 0; c < VEC; ++c) {
       const int64_t k = VEC * i + c;
+      // plain loads: each thread walks its node's VEC entries in separate instructions, so a
+      // streaming (evict-first) load would drop lines the neighbouring lanes read next (measured:
+      // 65 -> 77 us per launch at 3.1M dofs)
       x[k] += alpha * p[k];
       rv[c] = r[k] - alpha * q[k];
       r[k] = rv[c];
@@ -1383,14 +1412,18 @@ pcgx_update_bulk_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
       const int64_t d0 = pt * 96;
       async_proxy_fence();
       mbar_expect_tx(bar, G::STAGE);
-      bulk_load(st, xh + d0, G::VB, bar);
-      bulk_load(st + G::VB, xl + d0, G::VB, bar);
-      bulk_load(st + 2 * G::VB, rh + d0, G::VB, bar);
-      bulk_load(st + 3 * G::VB, rl + d0, G::VB, bar);
+      // L2 priorities by reuse distance: x, r and the preconditioner come back only in the next
+      // iteration's update (after a full matrix stream), so they go evict-first; q (written by the
+      // SpMV just before), p and the z written here are read again within this iteration.
+      const uint64_t pol = l2_evict_first_policy();
+      bulk_load_hint(st, xh + d0, G::VB, bar, pol);
+      bulk_load_hint(st + G::VB, xl + d0, G::VB, bar, pol);
+      bulk_load_hint(st + 2 * G::VB, rh + d0, G::VB, bar, pol);
+      bulk_load_hint(st + 3 * G::VB, rl + d0, G::VB, bar, pol);
       bulk_load(st + 4 * G::VB, qh + d0, G::VB, bar);
       bulk_load(st + 5 * G::VB, ql + d0, G::VB, bar);
       bulk_load(st + 6 * G::VB, pp + pt * 128, G::PB, bar);
-      if constexpr (PCW > 0) bulk_load(st + 6 * G::VB + G::PB, pc + pt * 32 * PCW, G::CB, bar);
+      if constexpr (PCW > 0) bulk_load_hint(st + 6 * G::VB + G::PB, pc + pt * 32 * PCW, G::CB, bar, pol);
       if constexpr (SYM) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) bulk_load(st + 6 * G::VB + G::PB + G::CB + c * 256, qT + c * qs + pt * 32, 256, bar);
@@ -1420,13 +1453,13 @@ pcgx_update_bulk_kernel(int64_t n_nodes, float* __restrict__ xh, float* __restri
         const int nl = o / 3, c = o - 3 * nl;
         const float2 pv = spp[nl * 4 + c];
         const df2 x = df_add(df2{sxh[o], sxl[o]}, df_mul(a, df2{pv.x, pv.y}));
-        xh[d0 + o] = x.h;
-        xl[d0 + o] = x.l;
+        __stcs(xh + d0 + o, x.h);   // streaming stores: next read one iteration later
+        __stcs(xl + d0 + o, x.l);
         df2 qv{sqh[o], sql[o]};
         if constexpr (SYM) qv = df_add(qv, df_from_bits(sqt[c * 32 + nl]));
         const df2 r = df_add(df2{srh[o], srl[o]}, df_mul(na, qv));
-        rh[d0 + o] = r.h;
-        rl[d0 + o] = r.l;
+        __stcs(rh + d0 + o, r.h);
+        __stcs(rl + d0 + o, r.l);
         srh[o] = r.h;
         srl[o] = r.l;
       }
@@ -1524,7 +1557,7 @@ __global__ void pcgx_direction3_kernel(int64_t n, const float* __restrict__ z, f
     const int64_t i = k / 3;
     const int64_t o = i * 4 + (k - 3 * i);
     const float2 pv = pp[o];
-    const df2 p = df_add(df2{z[k], 0.f}, df_mul(b, df2{pv.x, pv.y}));
+    const df2 p = df_add(df2{__ldcs(z + k), 0.f}, df_mul(b, df2{pv.x, pv.y}));   // z: last use
     pp[o] = make_float2(p.h, p.l);
   }
 }
@@ -1583,7 +1616,7 @@ __global__ void pcg_direction_kernel(int64_t n, T* p, const T* z, const KCtl* C)
   if (C->done) return;
   const T beta = T(C->beta);
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-    p[k] = z[k] + beta * p[k];
+    p[k] = __ldcs(z + k) + beta * p[k];   // z: last use
 }
 
 // BiCGStab (jax.scipy.sparse.linalg.bicgstab iteration).
@@ -1978,6 +2011,7 @@ static int launch_dfdf(const fem_pattern_t* pat, int64_t n_nodes, const float* v
     static int per_sm = 0;
     if (per_sm == 0) {
       cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BULK_WARPS * 32, smem) != cudaSuccess ||
           per_sm < 1)
         per_sm = 1;

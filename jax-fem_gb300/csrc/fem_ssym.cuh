@@ -216,8 +216,9 @@ spmv_ssym_bulk_kernel(SsGrid G, const float* __restrict__ vals, const int16_t* _
       unsigned char* st = ring + (size_t)stage * Gm::STAGE;
       async_proxy_fence();
       mbar_expect_tx(bars + stage, SS_STAGE_SLOTS * (Gm::VB + Gm::LB));
-      bulk_load(st, vals + pk * 9 * 32, SS_STAGE_SLOTS * Gm::VB, bars + stage);
-      bulk_load(st + SS_STAGE_SLOTS * Gm::VB, vlo + pk * 9 * 32, SS_STAGE_SLOTS * Gm::LB, bars + stage);
+      const uint64_t pol = l2_evict_first_policy();   // the matrix streams through L2 evict-first
+      bulk_load_hint(st, vals + pk * 9 * 32, SS_STAGE_SLOTS * Gm::VB, bars + stage, pol);
+      bulk_load_hint(st + SS_STAGE_SLOTS * Gm::VB, vlo + pk * 9 * 32, SS_STAGE_SLOTS * Gm::LB, bars + stage, pol);
     }
     pk += SS_STAGE_SLOTS;
     return true;
