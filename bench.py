@@ -287,7 +287,7 @@ def measured_peak():
 
 
 TRAFFIC_PROFILES = {
-    "df48": os.path.join(ROOT, "profiles", "spmv_sliced_dfdf_bulk_hex8_100x50x25.txt"),
+    "df48": os.path.join(ROOT, "profiles", "spmv_sliced_dfdf_bulk_hex8_160x80x40.txt"),
     "sym_df48": os.path.join(ROOT, "profiles", "spmv_sym_df48_bulk_hex8_100x50x25.txt"),
 }
 
