@@ -484,24 +484,36 @@ __global__ void __launch_bounds__(DFM_THREADS, 4) cell_matrix_df_kernel(const As
       const int pb = pa + pp;
       const int64_t ee = tile * CPB + cc;
       if (ee >= P.n_cells) continue;
-      float mh[9], ml[9];
+      // M accumulates on the paired FP32 instructions (df_acc2): rows i of columns (0, 1) as three
+      // pairs, (M02, M12) as a fourth, M22 alone -- 4 paired + 1 scalar product-accumulates per qp
+      float2 ah[3], al[3], bh = make_float2(0.f, 0.f), bl = bh;
+      float ch = 0.f, cl = 0.f;
 #pragma unroll
-      for (int v = 0; v < 9; ++v) { mh[v] = 0.f; ml[v] = 0.f; }
+      for (int i = 0; i < 3; ++i) ah[i] = al[i] = make_float2(0.f, 0.f);
 #pragma unroll 2
       for (int q = 0; q < NQ; ++q) {
         const float2* ma = sm + (cc * NQ + q) * GQ + pa * 3;
         const float2* gb = sg + (cc * NQ + q) * GQ + pb * 3;
         const float2 m0 = ma[0], m1 = ma[1], m2 = ma[2], g0 = gb[0], g1 = gb[1], g2 = gb[2];
-        const df2 m[3] = {df2{m0.x, m0.y}, df2{m1.x, m1.y}, df2{m2.x, m2.y}};
-        const df2 g[3] = {df2{g0.x, g0.y}, df2{g1.x, g1.y}, df2{g2.x, g2.y}};
+        const float2 gh01 = make_float2(g0.x, g1.x), ngh01 = make_float2(-g0.x, -g1.x), gl01 = make_float2(g0.y, g1.y);
+        const float2 mrow[3] = {m0, m1, m2};
 #pragma unroll
         for (int i = 0; i < 3; ++i)
-#pragma unroll
-          for (int j = 0; j < 3; ++j) df_acc(mh[i * 3 + j], ml[i * 3 + j], m[i], g[j]);
+          df_acc2(ah[i], al[i], make_float2(mrow[i].x, mrow[i].x), make_float2(mrow[i].y, mrow[i].y), gh01, ngh01,
+                  gl01);
+        df_acc2(bh, bl, make_float2(m0.x, m1.x), make_float2(m0.y, m1.y), make_float2(g2.x, g2.x),
+                make_float2(-g2.x, -g2.x), make_float2(g2.y, g2.y));
+        df_acc(ch, cl, df2{m2.x, m2.y}, df2{g2.x, g2.y});
       }
       df2 M[9];
 #pragma unroll
-      for (int v = 0; v < 9; ++v) M[v] = df_fast(mh[v], ml[v]);
+      for (int i = 0; i < 3; ++i) {
+        M[i * 3 + 0] = df_fast(ah[i].x, al[i].x);
+        M[i * 3 + 1] = df_fast(ah[i].y, al[i].y);
+      }
+      M[2] = df_fast(bh.x, bl.x);
+      M[5] = df_fast(bh.y, bl.y);
+      M[8] = df_fast(ch, cl);
       const df2 tr = df_add(df_add(M[0], M[4]), M[8]);
       const int64_t na2 = sconn[cc * NN + pa], nb2 = sconn[cc * NN + pb];
       const int sab = P.slots[(ee * NN + pa) * NN + pb], sba = P.slots[(ee * NN + pb) * NN + pa];

@@ -89,6 +89,28 @@ __device__ __forceinline__ void df_acc(float& sh, float& sl, df2 a, df2 b) {
   sh = t;
 }
 
+// Two independent df_acc at once on Blackwell's paired FP32 instructions (FMUL2 / FFMA2 / FADD2,
+// sm_100+): component k of (sh, sl) accumulates ah.k * (xh.k + xl.k) + al.k * xh.k exactly as
+// df_acc does -- every paired operation rounds per component like its scalar form, and the
+// subtractions of the two-sum are FFMA2 with a -1 multiplier (exact).  nxh = -xh (negated once
+// per gathered x, reused across a block's rows) gives -p without a separate negation.
+__device__ __forceinline__ void df_acc2(float2& sh, float2& sl, float2 ah, float2 al, float2 xh, float2 nxh,
+                                        float2 xl) {
+  const float2 m1 = make_float2(-1.f, -1.f);
+  const float2 np = __fmul2_rn(ah, nxh);        // -p, p = fl(ah xh)
+  float2 e = __ffma2_rn(ah, xh, np);             // ah xh - p, exact
+  e = __ffma2_rn(ah, xl, e);
+  e = __ffma2_rn(al, xh, e);
+  const float2 t = __ffma2_rn(np, m1, sh);       // fl(sh + p)
+  const float2 bb = __ffma2_rn(sh, m1, t);       // fl(t - sh)
+  const float2 tb = __ffma2_rn(bb, m1, t);       // fl(t - bb)
+  const float2 d1 = __ffma2_rn(tb, m1, sh);      // fl(sh - (t - bb))
+  const float2 s = __fadd2_rn(np, bb);           // -fl(p - bb)
+  const float2 te = __ffma2_rn(s, m1, d1);       // the two-sum error fl(d1 + (p - bb))
+  sl = __fadd2_rn(sl, __fadd2_rn(te, e));
+  sh = t;
+}
+
 // FP32 -> FP64 from the bits (integer operations; GB300's FP64 pipe is ~1/64 of the FP32 rate):
 // exact for normal floats, FP32 subnormals become 0.
 __device__ __forceinline__ double f2d_bits(float f) {

@@ -722,6 +722,12 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
   float sh[VEC], sl[VEC];
 #pragma unroll
   for (int r = 0; r < VEC; ++r) { sh[r] = 0.f; sl[r] = 0.f; }
+  // The plain (non-SYM) vec-3 kernel accumulates a stage's two slots in two banks at once on the
+  // paired FP32 instructions (df_acc2), folded into sh / sl when the slice ends.
+  constexpr bool PAIR = !SYM && VEC == 3 && BULK_SLOTS == 2;
+  float2 ph[VEC], pl[VEC];
+#pragma unroll
+  for (int r = 0; r < VEC; ++r) ph[r] = pl[r] = make_float2(0.f, 0.f);
   float xih[VEC], xil[VEC];       // SYM: the row's own x
   bool first = true;              // SYM: next slot is the diagonal block
   auto load_own = [&]() {
@@ -752,9 +758,30 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
 #pragma unroll
       for (int t = 0; t < BULK_SLOTS; ++t)
         if (t < cnt) df_gather<VEC>(xp, sc[t * 32 + lane], xvh[t], xvl[t]);
+      if constexpr (PAIR) {
+        // the stage's two slots as the two components of paired FP32 operations
+        const bool two = cnt > 1;
+        float2 xh2[VEC], nxh2[VEC], xl2[VEC];
+#pragma unroll
+        for (int d = 0; d < VEC; ++d) {
+          const float h1 = two ? xvh[1][d] : 0.f, l1 = two ? xvl[1][d] : 0.f;
+          xh2[d] = make_float2(xvh[0][d], h1);
+          nxh2[d] = make_float2(-xvh[0][d], -h1);
+          xl2[d] = make_float2(xvl[0][d], l1);
+        }
+#pragma unroll
+        for (int v = 0; v < VV; ++v) {
+          const int r = v / VEC, d = v % VEC;
+          const float h0 = sv[v * 32 + lane];
+          const float l0 = df48_lo(h0, sq[v * 32 + lane]);
+          const float h1 = two ? sv[(VV + v) * 32 + lane] : 0.f;
+          const float l1 = two ? df48_lo(h1, sq[(VV + v) * 32 + lane]) : 0.f;
+          df_acc2(ph[r], pl[r], make_float2(h0, h1), make_float2(l0, l1), xh2[d], nxh2[d], xl2[d]);
+        }
+      }
 #pragma unroll
       for (int t = 0; t < BULK_SLOTS; ++t) {
-        if (t < cnt) {
+        if (!PAIR && t < cnt) {
           if constexpr (SYM) {
             float ah[VV], al[VV];
 #pragma unroll
@@ -808,6 +835,15 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
     }
     if (ck == ce) {  // slice finished: write its rows and the dot contribution
       const int64_t i = cs * 32 + lane;
+      if constexpr (PAIR) {   // fold the two banks into the row sums
+#pragma unroll
+        for (int r = 0; r < VEC; ++r) {
+          const df2 f = df_add(df_fast(ph[r].x, pl[r].x), df_fast(ph[r].y, pl[r].y));
+          sh[r] = f.h;
+          sl[r] = f.l;
+          ph[r] = pl[r] = make_float2(0.f, 0.f);
+        }
+      }
       if (i < n_nodes) {
 #pragma unroll
         for (int r = 0; r < VEC; ++r) {
