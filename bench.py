@@ -47,12 +47,14 @@ RTOL = 1e-8
 FULL_SIZE_PCG_ITERS = (2649, 2622)
 
 
-def workload_name(n):
+def workload_name(n, extent=None):
     nx, ny, nz = n
     cells = nx * ny * nz
     nodes = (nx + 1) * (ny + 1) * (nz + 1)
     nnz = 9 * (3 * nx + 1) * (3 * ny + 1) * (3 * nz + 1)
-    return (f"SIMP compliance TO iteration, HEX8 cantilever {nx}x{ny}x{nz} ({cells:,} cells, "
+    ext = tuple(extent or L)
+    dom = "" if ext == L else f" on [0,{ext[0]:g}]x[0,{ext[1]:g}]x[0,{ext[2]:g}]"
+    return (f"SIMP compliance TO iteration, HEX8 cantilever {nx}x{ny}x{nz}{dom} ({cells:,} cells, "
             f"{3 * nodes:,} dofs, CSR nnz {nnz:,})"), cells, nodes, nnz
 
 
@@ -68,9 +70,9 @@ def theta_step(theta0, k):
     return theta0 * (1.0 + 1e-4 * (k + 1))
 
 
-def make_problem(n):
+def make_problem(n, extent=None):
     import jax_fem_gb300 as jf
-    Lx, Ly, Lz = L
+    Lx, Ly, Lz = extent or L
     m = jf.box_mesh(*n, Lx, Ly, Lz)
     mesh = jf.Mesh(m.points, m.cells_dict["hexahedron"])
     left = lambda p: np.isclose(p[0], 0.0, atol=1e-5)
@@ -254,10 +256,18 @@ def assembly_roofline(prob, peak):
     res = torch.zeros(nd, dtype=torch.float64, device="cuda")
     s = torch.cuda.current_stream()
     out = {}
-    cases = (("matrix_df48", L_.FEM_OUT_MATRIX, L_.FEM_DF48, cells * per_cell + 16 * eng.nnz + 8 * (nd + 1) + nd),
-             ("matrix_fp64", L_.FEM_OUT_MATRIX, L_.FEM_F64, cells * per_cell + 16 * eng.nnz + 8 * (nd + 1) + nd),
-             ("residual_fp64", L_.FEM_OUT_RESIDUAL, L_.FEM_F64, cells * per_cell + 24 * nd + nd))
-    for name, outputs, prec, algo in cases:
+    # flops per cell of the isotropic node-pair tangent: per node pair a <= b and quadrature point
+    # m = mu g_a (3 mul) and M += m (x) g_b (9 FMA); per pair K_ab = cr M + M^T + tr(M) I (9 FMA +
+    # 9 add + trace); the residual: grad u (nn*3*3 FMA), the stress (~30), the row sums (nn*3*3 FMA)
+    n_pairs = nn * (nn + 1) // 2
+    mat_flops = cells * (n_pairs * nq * (3 + 18) + n_pairs * (27 + 2))
+    res_flops = cells * nq * (2 * nn * 9 + 30 + 2 * nn * 9)
+    cases = (("matrix_df48", L_.FEM_OUT_MATRIX, L_.FEM_DF48, cells * per_cell + 16 * eng.nnz + 8 * (nd + 1) + nd,
+              mat_flops),
+             ("matrix_fp64", L_.FEM_OUT_MATRIX, L_.FEM_F64, cells * per_cell + 16 * eng.nnz + 8 * (nd + 1) + nd,
+              mat_flops),
+             ("residual_fp64", L_.FEM_OUT_RESIDUAL, L_.FEM_F64, cells * per_cell + 24 * nd + nd, res_flops))
+    for name, outputs, prec, algo, flops in cases:
         def launch():
             call("fem_assemble", C.byref(eng.mesh), C.byref(ms), C.byref(eng.pattern), outputs, prec, ptr(u), None,
                  ptr(eng.bc_mask), L_.FEM_BC_SYMMETRIC, ptr(res), ptr(vals), None, stream_handle())
@@ -274,7 +284,7 @@ def assembly_roofline(prob, peak):
                 ts.append(ev[0].elapsed_time(ev[1]) / 1e3)
         t = float(np.median(ts))
         out[name] = {"seconds": t, "algorithmic_bytes": int(algo), "achieved_gbs": algo / t / 1e9,
-                     "frac": algo / t / 1e9 / peak}
+                     "frac": algo / t / 1e9 / peak, "flops": int(flops), "tflops": flops / t / 1e12}
     return out
 
 
@@ -741,6 +751,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, nargs=3, default=list(DEFAULT_SIZE))
+    ap.add_argument("--extent", type=float, nargs=3, default=list(L),
+                    help="box extents Lx Ly Lz (default the 2 x 1 x 0.5 cantilever; 1 1 1 with --size 100 100 100 "
+                         "is the 100^3 unit cube)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed_ssym", "mixed_sym"],
                     help="mixed-precision variant of the headline run (solver copy of the tangent)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
@@ -779,8 +792,8 @@ def main():
         dist.init_process_group("nccl")
 
     n = tuple(args.size)
-    name, cells, nodes, nnz = workload_name(n)
-    prob = make_problem(n)
+    name, cells, nodes, nnz = workload_name(n, tuple(args.extent))
+    prob = make_problem(n, tuple(args.extent))
     eng = prob._engine
     theta0 = theta_init(cells).cuda()
     peak, peak_kind = measured_peak()
@@ -865,7 +878,7 @@ def main():
 
     # ---- CPU baseline (rank 0, N=1) ----------------------------------------------
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu and tuple(args.extent) == L:   # the port builds the cantilever
         it_full = (its_64[0], its_64[1]) if fp64 is not None and len(its_64) >= 2 else \
             (FULL_SIZE_PCG_ITERS if n == DEFAULT_SIZE else _default_iters(n))
         try:
