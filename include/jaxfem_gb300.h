@@ -365,8 +365,12 @@ int fem_bicgstab(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t
                  int64_t* iterations, double* res_norm, int32_t* status, void* stream);
 
 /* Mixed-precision PCG with FP64 reliable updates.  precision FEM_F32 / FEM_SLICED_F32: FP32
- * matrix, FP32 vectors; FEM_DF48 / FEM_SLICED_DF48: DF48 matrix (double-float SpMV on FP32
- * pipes), FP64 vectors and dots.  The preconditioner pc32 is FP32 in all cases.
+ * matrix, FP32 vectors; FEM_DF48 / FEM_SLICED_DF48 / FEM_SYM_DF48 / FEM_SSYM_DF48: DF48 matrix
+ * (double-float SpMV on FP32 pipes), double-float vectors, dot partials reduced in double-float,
+ * FP64 scalars.  The preconditioner pc32 is FP32 in all cases (Jacobi: one float per dof; block
+ * Jacobi: the VEC x VEC inverse blocks, VEC^2 floats per node).  CG takes the matrix and the
+ * preconditioner as symmetric: with FEM_SLICED_DF48 and vec 3 the block inverses are applied
+ * through their upper triangles.
  * Solves the Dirichlet-eliminated system K_ff x_f = b_f (x_b = b_b on Dirichlet dofs)
  * where K is the tangent of `mat` at u_lin.  x (FP64, in/out) holds the initial guess.
  * When the FP32 recursive residual has fallen by `delta` since the last replacement,
