@@ -817,7 +817,7 @@ def main():
         s = torch.cuda.current_stream()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         l0 = lib.fem_kernel_launches()
-        if spmv_timer:   # CUDA events around the first SpMV of every 16-iteration chunk of the CG
+        if spmv_timer:   # CUDA events around the second SpMV of every 16-iteration chunk of the CG
             lib.fem_spmv_timing_start()
         e0.record(s)
         out = None
@@ -927,7 +927,7 @@ def main():
                                 "double-float on FP32 pipes)"),
                      "peak_kind": peak_kind, "algorithmic_bytes": f32.get("algorithmic_bytes"),
                      "launch_seconds": f32.get("seconds"),
-                     "timing": ("CUDA events around the first SpMV of every 16-iteration chunk inside the timed "
+                     "timing": ("CUDA events around the second SpMV of every 16-iteration chunk inside the timed "
                                 f"mixed steps ({spmv_in_loop.get('launches_timed', 0)} launches)"
                                 if spmv_in_loop.get("launches_timed") else "20 back-to-back launches"),
                      "isolated": {"seconds": isolated.get("seconds"), "achieved_gbs": isolated.get("achieved_gbs"),

@@ -397,8 +397,8 @@ int fem_axpy_f32_f64(double alpha, const float* x, double* y, int64_t n, void* s
 int fem_dot(int32_t precision, const void* x, const void* y, int64_t n, double* out,
             void* ws, size_t ws_bytes, void* stream);
 /* Measurement hook (no reference counterpart): between start and stop, the mixed CG
- * (fem_pcg_refined with FEM_SLICED_DF48 / FEM_SYM_DF48) brackets the first SpMV of every
- * 16-iteration chunk with CUDA events on its stream; stop returns the summed SpMV time and the
+ * (fem_pcg_refined with a DF48 format) brackets the second SpMV of every 16-iteration chunk
+ * (the first follows the host's poll) with CUDA events on its stream; stop returns the summed SpMV time and the
  * number of timed launches.  Process-wide state: not for concurrent solves. */
 int fem_spmv_timing_start(void);
 int fem_spmv_timing_stop(double* seconds, int64_t* samples);

@@ -118,11 +118,11 @@ def _precision(cfg):
 
 def _mixed_matrix_precision(precision, eng=None):
     """Solver copy of the tangent.  'mixed' / 'mixed_sliced': sliced DF48 (the fastest measured on
-    GB300: the SpMV streams at ~0.89 of the copy peak); 'mixed_ssym': the structured symmetric DF48
+    GB300: the SpMV streams at ~0.9 of the copy peak); 'mixed_ssym': the structured symmetric DF48
     layout (diagonal and upper stencil blocks, implicit columns; the transposed half in registers
     and warp shuffles) when the nodes form a box grid (eng.grid) and the tangent is symmetric,
-    sliced DF48 otherwise -- it moves 0.58x the bytes but its double-float arithmetic is issue
-    bound (456 us against 277 us per SpMV at 1M cells); 'mixed_sym': upper node blocks of the
+    sliced DF48 otherwise -- it moves 0.52x the bytes but its double-float arithmetic is issue
+    bound (456 us against 260-277 us per SpMV at 1M cells); 'mixed_sym': upper node blocks of the
     general pattern with the transposed half through FP64 atomics (slower on GB300: the atomics
     cost more than the bytes saved); sliced FP32 for 'mixed32'."""
     if precision == "mixed_sym" and eng is not None and eng.vec == 3 and getattr(eng._mat, "symmetric", False):
