@@ -1965,8 +1965,20 @@ struct SpmvTimer {
   int used = 0;          // pairs recorded since the last read-back
   double seconds = 0.0;  // summed durations
   int64_t samples = 0;
+  cudaEvent_t gev[2] = {};   // the pair recorded by a captured chunk (ChunkGraph), once per replay
+  bool graph_pending = false;
 };
 static SpmvTimer g_spmv_timer;
+
+// Record one of the captured chunk's pair while a ChunkGraph is being captured on st.
+static void spmv_timer_mark_graph(int end, cudaStream_t st) {
+  SpmvTimer& T = g_spmv_timer;
+  if (!T.on) return;
+  cudaEvent_t& e = T.gev[end];
+  if (!e) return;   // created before the capture (ChunkGraph::build)
+  // an external record node: a plain record inside a capture only orders the captured work
+  cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+}
 
 static void spmv_timer_mark(int end, cudaStream_t s) {
   SpmvTimer& T = g_spmv_timer;
@@ -1979,11 +1991,23 @@ static void spmv_timer_mark(int end, cudaStream_t s) {
 
 static void spmv_timer_collect() {
   SpmvTimer& T = g_spmv_timer;
+  if (T.graph_pending && T.gev[0] && T.gev[1]) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, T.gev[0], T.gev[1]) == cudaSuccess) {
+      T.seconds += 1e-3 * ms;
+      ++T.samples;
+    } else {
+      cudaGetLastError();   // a measurement miss must not surface as a later launch error
+    }
+  }
+  T.graph_pending = false;
   for (int k = 0; k < T.used; ++k) {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, T.ev[2 * k], T.ev[2 * k + 1]) == cudaSuccess) {
       T.seconds += 1e-3 * ms;
       ++T.samples;
+    } else {
+      cudaGetLastError();
     }
   }
   T.used = 0;
@@ -1992,10 +2016,65 @@ static void spmv_timer_collect() {
 static int poll(KCtl* C, cudaStream_t s, KCtl* host) {
   FEM_CUDA(cudaMemcpyAsync(host, C, sizeof(KCtl), cudaMemcpyDeviceToHost, s));
   FEM_CUDA(cudaStreamSynchronize(s));
-  if (g_spmv_timer.used) spmv_timer_collect();
+  if (g_spmv_timer.used || g_spmv_timer.graph_pending) spmv_timer_collect();
   if (host->fault) return fail(FEM_ERR_DEVICE, "a bounded device wait (bulk-copy barrier) ran out");
   return FEM_OK;
 }
+
+// One chunk of a Krylov loop captured as a CUDA graph and replayed.  The chunk's kernels are the
+// same launch after launch (fixed pointers; the scalars live in the control block), so one capture
+// per solve replaces 3 x CHUNK stream launches by one graph launch.  The capture runs on a private
+// non-blocking stream (the caller's stream may be the legacy default stream, which cannot be
+// captured); the replays go to the caller's stream.  Launch counts: the kernels recorded during
+// the capture did not run, so they are taken back and credited at every replay.
+struct ChunkGraph {
+  cudaGraphExec_t exec = nullptr;
+  uint64_t launches = 0;     // kernels per replay
+  bool timed = false;        // the capture recorded the SpMV timing pair
+  ChunkGraph() = default;
+  ChunkGraph(const ChunkGraph&) = delete;
+  ChunkGraph& operator=(const ChunkGraph&) = delete;
+  ~ChunkGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+  // launch_chunk(stream) launches one chunk and returns FEM_OK; false: no graph (plain launches)
+  template <class F>
+  bool build(F&& launch_chunk) {
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) { cudaGetLastError(); return false; }
+    const uint64_t l0 = fem_kernel_launches();
+    timed = g_spmv_timer.on;
+    for (int k = 0; k < 2 && timed; ++k)   // the timing pair exists before the capture records it
+      if (!g_spmv_timer.gev[k] && cudaEventCreate(&g_spmv_timer.gev[k]) != cudaSuccess) {
+        g_spmv_timer.gev[k] = nullptr;
+        timed = false;
+        cudaGetLastError();
+      }
+    bool ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    int rc = FEM_OK;
+    if (ok) rc = launch_chunk(cs);
+    cudaGraph_t g = nullptr;
+    if (ok) ok = cudaStreamEndCapture(cs, &g) == cudaSuccess && g != nullptr && rc == FEM_OK;
+    if (ok) ok = cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    const uint64_t captured = fem_kernel_launches() - l0;
+    note_launches(-(int)captured);
+    launches = captured;
+    if (!ok) {
+      if (exec) cudaGraphExecDestroy(exec);
+      exec = nullptr;
+    }
+    cudaGetLastError();   // a failed capture leaves its error behind
+    return ok;
+  }
+  int launch(cudaStream_t s) {
+    FEM_CUDA(cudaGraphLaunch(exec, s));
+    note_launches((int)launches);
+    if (timed && g_spmv_timer.on) g_spmv_timer.graph_pending = true;
+    return FEM_OK;
+  }
+};
 
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
@@ -2107,7 +2186,7 @@ static int launch_ssym(const fem_pattern_t* pat, const float* vhi, const int16_t
 template <int VEC, typename T, int PC>
 static int pcg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, const T* pc, const T* b, T* x,
                     double rtol, double atol, int64_t maxiter, void* ws, int64_t* iters, double* rnorm,
-                    int32_t* status, cudaStream_t s, int mfmt) {
+                    int32_t* status, cudaStream_t s, int mfmt, bool graphs = true) {
   const int64_t n = n_nodes * VEC;
   KWs w = carve(ws, n, sizeof(T) == 4 ? FEM_F32 : FEM_F64);
   T* r = reinterpret_cast<T*>(w.vecs);
@@ -2124,17 +2203,38 @@ static int pcg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, co
   if (rc) return rc;
   KCtl h;
   int64_t launched = 0;
+  auto run_iters = [&](cudaStream_t st, int k_count) -> int {
+    for (int k = 0; k < k_count; ++k) {
+      launch_spmv<VEC, T>(pat, n_nodes, vals, p, q, p, C, FIN_PCG_ALPHA, w.partials, 1, st, mfmt);
+      pcg_update_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, st>>>(n_nodes, x, r, z, p, q, pc, C,
+                                                                             w.partials, FIN_PCG_UPDATE);
+      note_launches(1);
+      pcg_direction_kernel<T><<<vec_grid(n), VTHREADS, 0, st>>>(n, p, z, C);
+      note_launches(1);
+    }
+    return FEM_OK;
+  };
+  // full chunks after the first replay one captured chunk (ChunkGraph); the allocation-free entry
+  // point keeps plain launches (instantiating a graph allocates)
+  ChunkGraph graph;
+  bool graph_tried = !graphs;
   while (true) {
     rc = poll(C, s, &h);
     if (rc) return rc;
     if (h.done || launched >= maxiter) break;
-    for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
-      launch_spmv<VEC, T>(pat, n_nodes, vals, p, q, p, C, FIN_PCG_ALPHA, w.partials, 1, s, mfmt);
-      pcg_update_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, x, r, z, p, q, pc, C, w.partials,
-                                                                            FIN_PCG_UPDATE);
-      note_launches(1);
-      pcg_direction_kernel<T><<<vec_grid(n), VTHREADS, 0, s>>>(n, p, z, C);
-      note_launches(1);
+    if (maxiter - launched >= CHUNK && launched > 0 && !graph_tried) {
+      graph_tried = true;
+      graph.build([&](cudaStream_t cs) { return run_iters(cs, CHUNK); });
+    }
+    if (graph.exec && maxiter - launched >= CHUNK) {
+      rc = graph.launch(s);
+      if (rc) return rc;
+      launched += CHUNK;
+    } else {
+      const int k_count = (int)std::min<int64_t>(CHUNK, maxiter - launched);
+      rc = run_iters(s, k_count);
+      if (rc) return rc;
+      launched += k_count;
     }
     rc = check_launch("pcg iteration");
     if (rc) return rc;
@@ -2456,6 +2556,36 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
     pcgx_start_kernel<VEC, PCK><<<gn, VTHREADS, 0, s>>>(n_nodes, rh, rl, z, pp, pck, 1, C, w.partials);
     note_launches(1);
     int64_t launched = 0;
+    // k_count iterations (SpMV, update, direction) on stream st; the timed pair brackets the second
+    // SpMV (the first follows the host poll on an idle GPU, so its bracket would hold the launch
+    // latency too)
+    auto run_iters = [&](cudaStream_t st, int k_count, bool captured) -> int {
+      for (int k = 0; k < k_count; ++k) {
+        if (k == 1) { if (captured) spmv_timer_mark_graph(0, st); else spmv_timer_mark(0, st); }
+        int r2;
+        if constexpr (MODE == DFX_SSYM)
+          r2 = launch_ssym(pat, vhi, vlo, pp, qh, ql, qT, C, FIN_PCG_ALPHA, w.partials, st);
+        else
+          r2 = launch_dfdf<VEC, SYM>(pat, n_nodes, vhi, vlo, pp, qh, ql, C, FIN_PCG_ALPHA, w.partials, st, qT);
+        if (r2) return r2;
+        if (k == 1) { if (captured) spmv_timer_mark_graph(1, st); else spmv_timer_mark(1, st); }
+        if constexpr (VEC == 3) {
+          if (!launch_update_bulk<PCK, SYM>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pck, C, w.partials,
+                                            FIN_PCGR_UPDATE, st, qT))
+            pcgx_update_tile_kernel<PCK, SYM><<<gt, VTHREADS, 0, st>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pck,
+                                                                       C, w.partials, FIN_PCGR_UPDATE, qT);
+          pcgx_direction3_kernel<<<gv, VTHREADS, 0, st>>>(n, z, pp, C);
+        } else {
+          pcgx_update_kernel<VEC, PC><<<gn, VTHREADS, 0, st>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
+                                                              w.partials, FIN_PCGR_UPDATE);
+          pcgx_direction_kernel<VEC><<<gn, VTHREADS, 0, st>>>(n_nodes, z, pp, C);
+        }
+        note_launches(2);
+      }
+      return FEM_OK;
+    };
+    ChunkGraph graph;
+    bool graph_tried = false;
     while (true) {
       rc = poll(C, s, &h);
       if (rc) return rc;
@@ -2492,28 +2622,21 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
         note_launches(1);
         break;
       }
-      for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
-        // timed: the chunk's second SpMV (the first follows the host poll on an idle GPU, so its
-        // bracket would hold the launch latency too)
-        if (k == 1) spmv_timer_mark(0, s);
-        if constexpr (MODE == DFX_SSYM)
-          rc = launch_ssym(pat, vhi, vlo, pp, qh, ql, qT, C, FIN_PCG_ALPHA, w.partials, s);
-        else
-          rc = launch_dfdf<VEC, SYM>(pat, n_nodes, vhi, vlo, pp, qh, ql, C, FIN_PCG_ALPHA, w.partials, s, qT);
+      if (maxiter - launched >= CHUNK && launched > 0 && !graph_tried) {
+        // the first chunk ran as plain launches (it set up the launchers' occupancy state); capture
+        // one full chunk for the rest of the solve
+        graph_tried = true;
+        graph.build([&](cudaStream_t cs) { return run_iters(cs, CHUNK, true); });
+      }
+      if (graph.exec && maxiter - launched >= CHUNK) {
+        rc = graph.launch(s);
         if (rc) return rc;
-        if (k == 1) spmv_timer_mark(1, s);
-        if constexpr (VEC == 3) {
-          if (!launch_update_bulk<PCK, SYM>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pck, C, w.partials,
-                                            FIN_PCGR_UPDATE, s, qT))
-            pcgx_update_tile_kernel<PCK, SYM><<<gt, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pck,
-                                                                      C, w.partials, FIN_PCGR_UPDATE, qT);
-          pcgx_direction3_kernel<<<gv, VTHREADS, 0, s>>>(n, z, pp, C);
-        } else {
-          pcgx_update_kernel<VEC, PC><<<gn, VTHREADS, 0, s>>>(n_nodes, xh, xl, rh, rl, z, pp, qh, ql, pc, C,
-                                                             w.partials, FIN_PCGR_UPDATE);
-          pcgx_direction_kernel<VEC><<<gn, VTHREADS, 0, s>>>(n_nodes, z, pp, C);
-        }
-        note_launches(2);
+        launched += CHUNK;
+      } else {
+        const int k_count = (int)std::min<int64_t>(CHUNK, maxiter - launched);
+        rc = run_iters(s, k_count, false);
+        if (rc) return rc;
+        launched += k_count;
       }
       rc = check_launch("pcg_dfx iteration");
       if (rc) return rc;
@@ -2755,7 +2878,7 @@ extern "C" int fem_krylov_workspace(int64_t n_dofs, int32_t precision, size_t* b
 template <typename T>
 static int solve_dispatch(bool bicg, const fem_pattern_t* pat, int64_t n_nodes, int vec, const void* vals, int pc_kind,
                           const void* pc, const void* b, void* x, double rtol, double atol, int64_t maxiter, void* ws,
-                          int64_t* it, double* rn, int32_t* st, cudaStream_t s, int mfmt) {
+                          int64_t* it, double* rn, int32_t* st, cudaStream_t s, int mfmt, bool graphs = true) {
   const T* V = (const T*)vals;
   const T* P = (const T*)pc;
   const T* B = (const T*)b;
@@ -2763,7 +2886,7 @@ static int solve_dispatch(bool bicg, const fem_pattern_t* pat, int64_t n_nodes, 
 #define FEM_SOLVE_CASE(VEC, PC)                                                                          \
   if (vec == VEC && pc_kind == PC)                                                                       \
     return bicg ? bicg_impl<VEC, T, PC>(pat, n_nodes, V, P, B, X, rtol, atol, maxiter, ws, it, rn, st, s, mfmt) \
-                : pcg_impl<VEC, T, PC>(pat, n_nodes, V, P, B, X, rtol, atol, maxiter, ws, it, rn, st, s, mfmt);
+                : pcg_impl<VEC, T, PC>(pat, n_nodes, V, P, B, X, rtol, atol, maxiter, ws, it, rn, st, s, mfmt, graphs);
   FEM_SOLVE_CASE(3, FEM_PC_NONE)
   FEM_SOLVE_CASE(3, FEM_PC_JACOBI)
   FEM_SOLVE_CASE(3, FEM_PC_BJACOBI)
@@ -3110,7 +3233,7 @@ extern "C" int fem_pcg_static(const fem_pattern_t* pat, int64_t n_nodes, int32_t
   cudaStream_t s = as_stream(stream);
   if (vec_f32(precision))
     return solve_dispatch<float>(false, pat, n_nodes, vec, vals, pc_kind, pc, b, x, rtol, atol, maxiter, ws,
-                                 iterations, res_norm, status, s, precision);
+                                 iterations, res_norm, status, s, precision, false);
   return solve_dispatch<double>(false, pat, n_nodes, vec, vals, pc_kind, pc, b, x, rtol, atol, maxiter, ws,
-                                iterations, res_norm, status, s, precision);
+                                iterations, res_norm, status, s, precision, false);
 }
