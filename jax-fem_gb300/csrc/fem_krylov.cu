@@ -2264,19 +2264,38 @@ static int bicg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, c
   if (rc) return rc;
   KCtl h;
   int64_t launched = 0;
+  auto run_iters = [&](cudaStream_t st, int k_count) -> int {
+    for (int k = 0; k < k_count; ++k) {
+      bicg_p_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, st>>>(n_nodes, r, p, q, phat, pc, C);
+      note_launches(1);
+      launch_spmv<VEC, T>(pat, n_nodes, vals, phat, q, rhat, C, FIN_BICG_ALPHA, w.partials, 1, st, mfmt);
+      bicg_s_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, st>>>(n_nodes, r, q, sv, shat, pc, C, w.partials);
+      note_launches(1);
+      launch_spmv<VEC, T>(pat, n_nodes, vals, shat, t, sv, C, FIN_BICG_OMEGA, w.partials, 2, st, mfmt);
+      bicg_update_kernel<T><<<vec_grid(n), VTHREADS, 0, st>>>(n, x, r, rhat, phat, sv, shat, t, C, w.partials);
+      note_launches(1);
+    }
+    return FEM_OK;
+  };
+  ChunkGraph graph;   // full chunks after the first replay one captured chunk
+  bool graph_tried = false;
   while (true) {
     rc = poll(C, s, &h);
     if (rc) return rc;
     if (h.done || launched >= maxiter) break;
-    for (int k = 0; k < CHUNK && launched < maxiter; ++k, ++launched) {
-      bicg_p_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, p, q, phat, pc, C);
-      note_launches(1);
-      launch_spmv<VEC, T>(pat, n_nodes, vals, phat, q, rhat, C, FIN_BICG_ALPHA, w.partials, 1, s, mfmt);
-      bicg_s_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, s>>>(n_nodes, r, q, sv, shat, pc, C, w.partials);
-      note_launches(1);
-      launch_spmv<VEC, T>(pat, n_nodes, vals, shat, t, sv, C, FIN_BICG_OMEGA, w.partials, 2, s, mfmt);
-      bicg_update_kernel<T><<<vec_grid(n), VTHREADS, 0, s>>>(n, x, r, rhat, phat, sv, shat, t, C, w.partials);
-      note_launches(1);
+    if (maxiter - launched >= CHUNK && launched > 0 && !graph_tried) {
+      graph_tried = true;
+      graph.build([&](cudaStream_t cs) { return run_iters(cs, CHUNK); });
+    }
+    if (graph.exec && maxiter - launched >= CHUNK) {
+      rc = graph.launch(s);
+      if (rc) return rc;
+      launched += CHUNK;
+    } else {
+      const int k_count = (int)std::min<int64_t>(CHUNK, maxiter - launched);
+      rc = run_iters(s, k_count);
+      if (rc) return rc;
+      launched += k_count;
     }
     rc = check_launch("bicgstab iteration");
     if (rc) return rc;
