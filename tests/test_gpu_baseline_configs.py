@@ -81,14 +81,16 @@ def test_config1_cube_fp64_vs_direct_and_pcg_iterates(cuda):
     err = np.abs(sol - ref).max() / np.abs(ref).max()
     assert err <= kappa * 1e-12, (err, kappa)
     assert err <= 1e-10
-    # the PCG iterates: GPU fem_pcg with maxiter k vs the restated PCG on the same matrix and RHS
+    # the PCG iterates: GPU fem_pcg with maxiter k vs the restated PCG on the same matrix and RHS;
+    # k = 48 and 64 run their second to fourth 16-iteration chunks as replays of a captured CUDA
+    # graph, so those iterates also pin the graph path against the plain launches
     z = torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda)
     A = eng.tangent(z, jf._lib.FEM_F64, jf._lib.FEM_BC_SYMMETRIC, cache=False)
     b = -eng.residual(z, apply_bc=True)
     A_cpu = A.to_scipy()
     b_cpu = b.cpu().numpy()
     M = _bjacobi(A_cpu)
-    for k in (1, 5, 25):
+    for k in (1, 5, 25, 48, 64):
         x = torch.zeros_like(b)
         eng.krylov("cg", A, b, x, jf._lib.FEM_PC_BJACOBI, 1e-30, 0.0, k)
         xo, it = osolve.pcg(A_cpu, b_cpu, Minv=M, rtol=1e-30, maxiter=k)
