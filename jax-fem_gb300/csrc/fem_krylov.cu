@@ -2074,6 +2074,28 @@ struct ChunkGraph {
     if (timed && g_spmv_timer.on) g_spmv_timer.graph_pending = true;
     return FEM_OK;
   }
+  // The next chunk of a loop: a replay of the captured chunk while a full chunk remains (captured
+  // on the first call after a plain first chunk, which also set up the launchers' occupancy
+  // state), plain launches otherwise.  run_iters(stream, k, captured) launches k iterations.
+  template <class F>
+  int step(cudaStream_t s, int64_t& launched, int64_t maxiter, F&& run_iters) {
+    if (!tried && launched > 0 && maxiter - launched >= CHUNK) {
+      tried = true;
+      build([&](cudaStream_t cs) { return run_iters(cs, CHUNK, true); });
+    }
+    if (exec && maxiter - launched >= CHUNK) {
+      const int rc = launch(s);
+      if (rc) return rc;
+      launched += CHUNK;
+      return FEM_OK;
+    }
+    const int k = (int)std::min<int64_t>(CHUNK, maxiter - launched);
+    const int rc = run_iters(s, k, false);
+    if (rc) return rc;
+    launched += k;
+    return FEM_OK;
+  }
+  bool tried = false;   // set to skip graphs (the allocation-free entry point)
 };
 
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
@@ -2203,7 +2225,7 @@ static int pcg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, co
   if (rc) return rc;
   KCtl h;
   int64_t launched = 0;
-  auto run_iters = [&](cudaStream_t st, int k_count) -> int {
+  auto run_iters = [&](cudaStream_t st, int k_count, bool) -> int {
     for (int k = 0; k < k_count; ++k) {
       launch_spmv<VEC, T>(pat, n_nodes, vals, p, q, p, C, FIN_PCG_ALPHA, w.partials, 1, st, mfmt);
       pcg_update_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, st>>>(n_nodes, x, r, z, p, q, pc, C,
@@ -2217,25 +2239,13 @@ static int pcg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, co
   // full chunks after the first replay one captured chunk (ChunkGraph); the allocation-free entry
   // point keeps plain launches (instantiating a graph allocates)
   ChunkGraph graph;
-  bool graph_tried = !graphs;
+  graph.tried = !graphs;
   while (true) {
     rc = poll(C, s, &h);
     if (rc) return rc;
     if (h.done || launched >= maxiter) break;
-    if (maxiter - launched >= CHUNK && launched > 0 && !graph_tried) {
-      graph_tried = true;
-      graph.build([&](cudaStream_t cs) { return run_iters(cs, CHUNK); });
-    }
-    if (graph.exec && maxiter - launched >= CHUNK) {
-      rc = graph.launch(s);
-      if (rc) return rc;
-      launched += CHUNK;
-    } else {
-      const int k_count = (int)std::min<int64_t>(CHUNK, maxiter - launched);
-      rc = run_iters(s, k_count);
-      if (rc) return rc;
-      launched += k_count;
-    }
+    rc = graph.step(s, launched, maxiter, run_iters);
+    if (rc) return rc;
     rc = check_launch("pcg iteration");
     if (rc) return rc;
   }
@@ -2264,7 +2274,7 @@ static int bicg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, c
   if (rc) return rc;
   KCtl h;
   int64_t launched = 0;
-  auto run_iters = [&](cudaStream_t st, int k_count) -> int {
+  auto run_iters = [&](cudaStream_t st, int k_count, bool) -> int {
     for (int k = 0; k < k_count; ++k) {
       bicg_p_kernel<VEC, T, PC><<<vec_grid(n_nodes), VTHREADS, 0, st>>>(n_nodes, r, p, q, phat, pc, C);
       note_launches(1);
@@ -2277,26 +2287,13 @@ static int bicg_impl(const fem_pattern_t* pat, int64_t n_nodes, const T* vals, c
     }
     return FEM_OK;
   };
-  ChunkGraph graph;   // full chunks after the first replay one captured chunk
-  bool graph_tried = false;
+  ChunkGraph graph;
   while (true) {
     rc = poll(C, s, &h);
     if (rc) return rc;
     if (h.done || launched >= maxiter) break;
-    if (maxiter - launched >= CHUNK && launched > 0 && !graph_tried) {
-      graph_tried = true;
-      graph.build([&](cudaStream_t cs) { return run_iters(cs, CHUNK); });
-    }
-    if (graph.exec && maxiter - launched >= CHUNK) {
-      rc = graph.launch(s);
-      if (rc) return rc;
-      launched += CHUNK;
-    } else {
-      const int k_count = (int)std::min<int64_t>(CHUNK, maxiter - launched);
-      rc = run_iters(s, k_count);
-      if (rc) return rc;
-      launched += k_count;
-    }
+    rc = graph.step(s, launched, maxiter, run_iters);
+    if (rc) return rc;
     rc = check_launch("bicgstab iteration");
     if (rc) return rc;
   }
@@ -2604,7 +2601,6 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
       return FEM_OK;
     };
     ChunkGraph graph;
-    bool graph_tried = false;
     while (true) {
       rc = poll(C, s, &h);
       if (rc) return rc;
@@ -2641,22 +2637,8 @@ static int pcg_dfx_impl(const fem_pattern_t* pat, int64_t n_nodes, const void* v
         note_launches(1);
         break;
       }
-      if (maxiter - launched >= CHUNK && launched > 0 && !graph_tried) {
-        // the first chunk ran as plain launches (it set up the launchers' occupancy state); capture
-        // one full chunk for the rest of the solve
-        graph_tried = true;
-        graph.build([&](cudaStream_t cs) { return run_iters(cs, CHUNK, true); });
-      }
-      if (graph.exec && maxiter - launched >= CHUNK) {
-        rc = graph.launch(s);
-        if (rc) return rc;
-        launched += CHUNK;
-      } else {
-        const int k_count = (int)std::min<int64_t>(CHUNK, maxiter - launched);
-        rc = run_iters(s, k_count, false);
-        if (rc) return rc;
-        launched += k_count;
-      }
+      rc = graph.step(s, launched, maxiter, run_iters);
+      if (rc) return rc;
       rc = check_launch("pcg_dfx iteration");
       if (rc) return rc;
     }
