@@ -27,7 +27,11 @@ namespace fem {
 constexpr int VTHREADS = 256;      // vector kernels
 constexpr int SPMV_THREADS = 256;  // 8 warps = 8 node rows per CTA
 constexpr int MAX_PARTIAL_BLOCKS = 8192;
-constexpr int CHUNK = 16;
+// Iterations launched between two host polls of the control block (one replayed graph per chunk)
+#ifndef FEM_CHUNK
+#define FEM_CHUNK 16
+#endif
+constexpr int CHUNK = FEM_CHUNK;
 
 struct KCtl {
   double rho, rho_prev, alpha, beta, omega, thresh2, rr, bb, d0, d1, ss;
