@@ -103,6 +103,29 @@ def test_widened_entry_points_validate_arguments(lib):
     assert "J2" in L.last_error() or "NULL" in L.last_error() or "mesh" in L.last_error()
 
 
+def test_geometry_cache_and_df_assembly_validate_arguments(lib):
+    """fem_cell_geometry and the FEM_DF48 assembly precision reject bad arguments before touching
+    the device: NULL outputs, a mesh whose geometry cache sets only one of its two arrays, an
+    assembly precision outside FP32 / FP64 / DF48."""
+    import ctypes as C
+    import jax_fem_gb300 as jf
+    L = jf._lib
+    empty = L.FemMesh(L.FEM_HEX8, 3, 0, 0, None, None)
+    assert lib.fem_cell_geometry(C.byref(empty), None, None, None) == L.FEM_ERR_ARG
+    assert "NULL" in L.last_error()
+    buf = (C.c_double * 8)()
+    assert lib.fem_cell_geometry(C.byref(empty), buf, buf, None) == L.FEM_OK    # no cells: nothing to do
+    half = L.FemMesh(L.FEM_HEX8, 3, 8, 1, C.addressof(buf), C.addressof(buf), C.addressof(buf), None)
+    mat = L.FemMaterial() if hasattr(L, "FemMaterial") else None
+    if mat is not None:
+        rc = lib.fem_assemble(C.byref(half), C.byref(mat), None, L.FEM_OUT_RESIDUAL, L.FEM_F64, buf, None, None,
+                              L.FEM_BC_NONE, buf, None, None, None)
+        assert rc == L.FEM_ERR_ARG and "shape_grads" in L.last_error()
+        rc = lib.fem_assemble(C.byref(empty), C.byref(mat), None, L.FEM_OUT_MATRIX, L.FEM_SLICED_DF48, None, None,
+                              None, L.FEM_BC_NONE, None, None, None, None)
+        assert rc == L.FEM_ERR_ARG and "precision" in L.last_error()
+
+
 def test_element_tables_match_oracle(lib):
     from jax_fem_gb300 import basis
     from oracle import basis as ob
