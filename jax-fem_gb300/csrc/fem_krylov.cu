@@ -17,6 +17,7 @@
 // iterations; no kernel ever waits on another.
 #include <cmath>
 #include <mutex>
+#include <type_traits>
 
 #include "fem_common.cuh"
 #include "fem_df.cuh"
@@ -763,25 +764,31 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
       for (int t = 0; t < BULK_SLOTS; ++t)
         if (t < cnt) df_gather<VEC>(xp, sc[t * 32 + lane], xvh[t], xvl[t]);
       if constexpr (PAIR) {
-        // the stage's two slots as the two components of paired FP32 operations
-        const bool two = cnt > 1;
-        float2 xh2[VEC], nxh2[VEC], xl2[VEC];
+        // the stage's two slots as the two components of paired FP32 operations; a stage with one
+        // slot (a slice's odd last one) pairs it with zeros -- a warp-uniform branch, so the full
+        // stages carry no per-value selects
+        auto pair_stage = [&](auto two_c) {
+          constexpr bool TWO = decltype(two_c)::value;
+          float2 xh2[VEC], nxh2[VEC], xl2[VEC];
 #pragma unroll
-        for (int d = 0; d < VEC; ++d) {
-          const float h1 = two ? xvh[1][d] : 0.f, l1 = two ? xvl[1][d] : 0.f;
-          xh2[d] = make_float2(xvh[0][d], h1);
-          nxh2[d] = make_float2(-xvh[0][d], -h1);
-          xl2[d] = make_float2(xvl[0][d], l1);
-        }
+          for (int d = 0; d < VEC; ++d) {
+            const float h1 = TWO ? xvh[1][d] : 0.f, l1 = TWO ? xvl[1][d] : 0.f;
+            xh2[d] = make_float2(xvh[0][d], h1);
+            nxh2[d] = make_float2(-xvh[0][d], -h1);
+            xl2[d] = make_float2(xvl[0][d], l1);
+          }
 #pragma unroll
-        for (int v = 0; v < VV; ++v) {
-          const int r = v / VEC, d = v % VEC;
-          const float h0 = sv[v * 32 + lane];
-          const float l0 = df48_lo(h0, sq[v * 32 + lane]);
-          const float h1 = two ? sv[(VV + v) * 32 + lane] : 0.f;
-          const float l1 = two ? df48_lo(h1, sq[(VV + v) * 32 + lane]) : 0.f;
-          df_acc2(ph[r], pl[r], make_float2(h0, h1), make_float2(l0, l1), xh2[d], nxh2[d], xl2[d]);
-        }
+          for (int v = 0; v < VV; ++v) {
+            const int r = v / VEC, d = v % VEC;
+            const float h0 = sv[v * 32 + lane];
+            const float l0 = df48_lo(h0, sq[v * 32 + lane]);
+            const float h1 = TWO ? sv[(VV + v) * 32 + lane] : 0.f;
+            const float l1 = TWO ? df48_lo(h1, sq[(VV + v) * 32 + lane]) : 0.f;
+            df_acc2(ph[r], pl[r], make_float2(h0, h1), make_float2(l0, l1), xh2[d], nxh2[d], xl2[d]);
+          }
+        };
+        if (cnt > 1) pair_stage(std::true_type{});
+        else pair_stage(std::false_type{});
       }
 #pragma unroll
       for (int t = 0; t < BULK_SLOTS; ++t) {
