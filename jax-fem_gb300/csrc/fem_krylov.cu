@@ -2085,15 +2085,12 @@ struct ChunkGraph {
     if (timed && g_spmv_timer.on) g_spmv_timer.graph_pending = true;
     return FEM_OK;
   }
-  // The next chunk of a loop: a replay of the captured chunk while a full chunk remains (captured
-  // on the first call after a plain first chunk, which also set up the launchers' occupancy
-  // state), plain launches otherwise.  run_iters(stream, k, captured) launches k iterations.
+  // The next chunk of a loop: a replay of the captured chunk while a full chunk remains, plain
+  // launches otherwise.  The capture follows the first plain chunk (whose launches set up the
+  // launchers' occupancy state) as soon as it is queued, so the host captures and instantiates
+  // while the GPU runs that chunk.  run_iters(stream, k, captured) launches k iterations.
   template <class F>
   int step(cudaStream_t s, int64_t& launched, int64_t maxiter, F&& run_iters) {
-    if (!tried && launched > 0 && maxiter - launched >= CHUNK) {
-      tried = true;
-      build([&](cudaStream_t cs) { return run_iters(cs, CHUNK, true); });
-    }
     if (exec && maxiter - launched >= CHUNK) {
       const int rc = launch(s);
       if (rc) return rc;
@@ -2104,6 +2101,10 @@ struct ChunkGraph {
     const int rc = run_iters(s, k, false);
     if (rc) return rc;
     launched += k;
+    if (!tried && maxiter - launched >= CHUNK) {
+      tried = true;
+      build([&](cudaStream_t cs) { return run_iters(cs, CHUNK, true); });
+    }
     return FEM_OK;
   }
   bool tried = false;   // set to skip graphs (the allocation-free entry point)
