@@ -2051,6 +2051,8 @@ struct ChunkGraph {
   // launch_chunk(stream) launches one chunk and returns FEM_OK; false: no graph (plain launches)
   template <class F>
   bool build(F&& launch_chunk) {
+    // an error left by the launches queued just before stays for the caller's check_launch
+    if (cudaPeekAtLastError() != cudaSuccess) return false;
     cudaStream_t cs = nullptr;
     if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) { cudaGetLastError(); return false; }
     const uint64_t l0 = fem_kernel_launches();
