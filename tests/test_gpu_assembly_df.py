@@ -106,6 +106,10 @@ def test_df_tangent_simp_hex8(cuda, bc_mode):
     assert Kdf.data_ptr() != K64.data_ptr()
     err = (Kdf - K64).abs().max().item() / K64.abs().max().item()
     assert 0 < err <= 1e-13, err     # computed differently (0 would mean the FP64 kernel ran)
+    # without the geometry cache (a mesh too large for it) the double-float request falls back to
+    # the FP64 kernel and still gives the tangent (the atomics' order makes equality bitwise loose)
+    Kfb = _without_cache(eng, lambda: eng.tangent(z, L.FEM_F64, bc_mode, cache=False, df_source=True).data.clone())
+    assert (Kfb - K64).abs().max().item() <= 1e-13 * K64.abs().max().item()
 
 
 def test_df_tangent_linear_elastic_tet10_tet4(cuda):
