@@ -73,7 +73,8 @@ def _bc_values(fn, pts):
             elif vv.shape != (len(pts),):
                 raise ValueError
             probe = np.unique(np.linspace(0, len(pts) - 1, min(len(pts), 5)).astype(np.int64))
-            if not all(abs(float(vv[p]) - float(fn(pts[p]))) <= 1e-12 * (abs(float(vv[p])) + 1.0) for p in probe):
+            val = lambda t: float(torch.as_tensor(t).detach())   # compare values, leave the graph alone
+            if not all(abs(val(vv[p]) - val(fn(pts[p]))) <= 1e-12 * (abs(val(vv[p])) + 1.0) for p in probe):
                 raise ValueError
             return vv.to(torch.float64)
         except Exception:  # noqa: BLE001 -- per point
