@@ -717,9 +717,10 @@ def mma_update_bench(args):
     cpu = None
     if not args.no_cpu:
         from oracle import mma as omma
+        t0 = time.perf_counter()     # centroids, volume and neighbour search, as the GPU build
         cent = np.mean(fe.points[fe.cells], axis=1)
-        t0 = time.perf_counter()
-        Ho, Hso, _ = omma.filter_kd_tree(cent, M._cell_volume(fe))
+        Ho, Hso, _ = omma.filter_kd_tree(cent, omma.cell_volume(fe.points, fe.cells, fe.shape_grads_ref,
+                                                                fe.quad_weights))
         t_cpu_build = time.perf_counter() - t0
         r, d0, dv = rho.cpu().numpy().reshape(-1), dJ.cpu().numpy().reshape(-1), dvc.cpu().numpy().reshape(1, -1)
         t0 = time.perf_counter()

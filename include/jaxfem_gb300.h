@@ -210,7 +210,7 @@ int fem_pattern_scalar(int64_t n_nodes, int32_t vec, const int64_t* block_ptr, c
  * Replaces jax_fem/fe.py:112-218 (shape grads, JxW, physical quad points,
  * face Nanson scale) and the u-independent parts of the mass / surface
  * kernels jax_fem/problem.py:216-259. */
-int fem_quad_points(const fem_mesh_t* mesh, double* x_out /* (n_cells,nq,3) */,
+int fem_quad_points(const fem_mesh_t* mesh, double* x_out /* (n_cells,nq,3) or NULL */,
                     double* jxw_out /* (n_cells,nq) or NULL */, void* stream);
 /* Physical shape gradients (n_cells, nq, nodes_per_cell, 3) and JxW (n_cells, nq) in FP64
  * (fe.py:112-141 get_shape_grads, kept by problem.py:130-147 initialize_geometric_quantities):

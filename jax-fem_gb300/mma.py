@@ -45,16 +45,21 @@ class Filter:
         return out
 
 
-def _cell_volume(fe, chunk=200000):
-    """sum of JxW over all cells (fe.JxW.sum() in mma.py:36), evaluated on the host in chunks."""
-    dN = np.asarray(fe.shape_grads_ref)
-    w = np.asarray(fe.quad_weights)
-    V = 0.0
+def _cell_volume(fe, chunk=1 << 22):
+    """Sum of JxW over all cells (fe.JxW.sum() in mma.py:36): JxW = det J w_q by fem_quad_points
+    on the device, in chunks of cells whose sums are added in order."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    coords = torch.as_tensor(np.asarray(fe.points), dtype=torch.float64, device=dev).contiguous()
+    conn = torch.as_tensor(np.asarray(fe.cells), dtype=torch.int32, device=dev).contiguous()
+    jxw = torch.empty(min(chunk, max(fe.num_cells, 1)) * fe.num_quads, dtype=torch.float64, device=dev)
+    V = torch.zeros((), dtype=torch.float64, device=dev)
     for c0 in range(0, fe.num_cells, chunk):
-        X = np.asarray(fe.points)[np.asarray(fe.cells)[c0:c0 + chunk]]
-        J = np.einsum("cnd,qne->cqde", X, dN)
-        V += float((np.linalg.det(J) * w[None, :]).sum())
-    return V
+        nc = min(chunk, fe.num_cells - c0)
+        mesh = _lib.FemMesh(fe.elem_id, 1, fe.num_total_nodes, nc, coords.data_ptr(), conn[c0].data_ptr(), None,
+                            None)
+        call("fem_quad_points", C.byref(mesh), None, ptr(jxw), _stream())
+        V += jxw[:nc * fe.num_quads].sum()
+    return float(V)
 
 
 def compute_filter_kd_tree(fe, num_nbs=NUM_NBS):

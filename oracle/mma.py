@@ -166,6 +166,23 @@ def mmasub(it, xval, xold1, xold2, low, upp, xmin, xmax, move, f0val, df0dx, fva
     return x, low, upp
 
 
+def cell_volume(points, cells, shape_grads_ref, quad_weights, chunk=1 << 18):
+    """fe.JxW.sum() (mma.py:36), with JxW = det(J) w_q and J = sum_a x_a (x) dN_a/dxi (fe.py:112-141),
+    per chunk of cells: J by one contraction over the cell's nodes, det J by the cofactor expansion
+    along its first row."""
+    dN = np.asarray(shape_grads_ref, dtype=np.float64)           # (nq, nn, 3)
+    w = np.asarray(quad_weights, dtype=np.float64)
+    V = 0.0
+    for c0 in range(0, len(cells), chunk):
+        X = np.asarray(points, dtype=np.float64)[np.asarray(cells)[c0:c0 + chunk]]   # (c, nn, 3)
+        J = np.tensordot(X, dN, axes=([1], [1])).transpose(0, 2, 1, 3)               # (c, nq, 3, 3)
+        det = (J[..., 0, 0] * (J[..., 1, 1] * J[..., 2, 2] - J[..., 1, 2] * J[..., 2, 1])
+               - J[..., 0, 1] * (J[..., 1, 0] * J[..., 2, 2] - J[..., 1, 2] * J[..., 2, 0])
+               + J[..., 0, 2] * (J[..., 1, 0] * J[..., 2, 1] - J[..., 1, 1] * J[..., 2, 0]))
+        V += float((det * w).sum())
+    return V
+
+
 def filter_kd_tree(centroids, volume, dim=3, num_nbs=20):
     """mma.py:27-57: rmin = 1.5 (V / n_cells)^(1/dim); H[i, j] = max(rmin - |c_i - c_j|, 0) over
     the num_nbs nearest centroids of c_i; Hs = row sums.  Returns (H as scipy CSR, Hs)."""

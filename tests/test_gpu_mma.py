@@ -40,8 +40,9 @@ def _jittered_box(nx, ny, nz, amp, seed):
 
 @pytest.mark.parametrize("amp", [0.0, 0.15])
 def test_filter_matches_kd_tree(cuda, amp):
-    """compute_filter_kd_tree on a uniform and on a jittered HEX8 mesh (9x7x5): the GPU filter's
-    weights and row sums equal the oracle's k-d tree filter to 1e-14."""
+    """compute_filter_kd_tree on a uniform and on a jittered HEX8 mesh (9x7x5): the domain volume
+    (JxW summed on the device) equals the oracle's to 1e-14, and the GPU filter's weights and row
+    sums equal the oracle's k-d tree filter to 1e-14."""
     import jax_fem_gb300 as jf
 
     class P(jf.Problem):
@@ -54,9 +55,10 @@ def test_filter_matches_kd_tree(cuda, amp):
     M = _mma_mod()
     H, Hs = M.compute_filter_kd_tree(fe)
     cent = np.mean(fe.points[fe.cells], axis=1)
-    V = M._cell_volume(fe)
+    V = omma.cell_volume(fe.points, fe.cells, fe.shape_grads_ref, fe.quad_weights)
+    assert abs(M._cell_volume(fe) - V) <= 1e-14 * V
     Ho, Hso, rmin = omma.filter_kd_tree(cent, V)
-    assert abs(H.rmin - rmin) <= 1e-15 * rmin
+    assert abs(H.rmin - rmin) <= 1e-14 * rmin
     np.testing.assert_allclose(_dense(H, fe.num_cells), Ho.toarray(), rtol=0, atol=1e-14)
     np.testing.assert_allclose(Hs.cpu().numpy(), Hso, rtol=1e-14, atol=0)
 
@@ -102,7 +104,8 @@ def test_filter_products_match_oracle(cuda):
     fe = prob.fes[0]
     M = _mma_mod()
     H, Hs = M.compute_filter_kd_tree(fe)
-    Ho, Hso, _ = omma.filter_kd_tree(np.mean(fe.points[fe.cells], axis=1), M._cell_volume(fe))
+    Ho, Hso, _ = omma.filter_kd_tree(np.mean(fe.points[fe.cells], axis=1),
+                                   omma.cell_volume(fe.points, fe.cells, fe.shape_grads_ref, fe.quad_weights))
     rng = np.random.default_rng(5)
     n = fe.num_cells
     rho = rng.uniform(0.0005, 1.0, (n, 1))
@@ -195,7 +198,8 @@ def test_optimize_three_iterations_matches_oracle_loop(cuda):
     designs.append(rho.cpu().numpy().reshape(-1))
 
     # the same loop with the oracle's filter and MMA
-    Ho, Hso, _ = omma.filter_kd_tree(np.mean(fe.points[fe.cells], axis=1), M._cell_volume(fe))
+    Ho, Hso, _ = omma.filter_kd_tree(np.mean(fe.points[fe.cells], axis=1),
+                                   omma.cell_volume(fe.points, fe.cells, fe.shape_grads_ref, fe.quad_weights))
     x = rho_ini.reshape(-1).copy()
     xold1, xold2 = x.copy(), x.copy()
     low, upp = np.ones(n), np.ones(n)

@@ -2,6 +2,7 @@
 the reference ships no MMA test, so the oracle is checked against a convex problem with an
 analytic optimum and against the filter's closed-form weights on a uniform grid."""
 import numpy as np
+import pytest
 
 from oracle import mma as omma
 
@@ -41,6 +42,37 @@ def test_oracle_mma_converges_to_kkt_point():
     err = np.abs(x - ref)
     assert np.median(err) < 1e-5 and err.max() < 1e-3
     assert abs(x.mean() / vf - 1.0) < 1e-5
+
+
+@pytest.mark.parametrize("ele", ["HEX8", "TET4", "TET10"])
+def test_oracle_cell_volume_tiles_the_box(ele):
+    """The cells of a box mesh tile the box, so sum JxW = Lx Ly Lz: with the interior nodes moved
+    for HEX8 (the 2x2x2 rule integrates det J of a trilinear map exactly) and TET4 (det J constant
+    per cell), on the affine mesh for TET10; the jittered TET10 sum equals the oracle FE's JxW."""
+    import jax_fem_gb300 as jf
+    from jax_fem_gb300 import basis
+    from oracle import fem as ofem
+    nx, ny, nz, Lx, Ly, Lz = 5, 4, 3, 1.0, 0.8, 0.6
+    if ele == "HEX8":
+        m = jf.box_mesh(nx, ny, nz, Lx, Ly, Lz)
+        pts, cells = np.array(m.points), np.asarray(m.cells_dict["hexahedron"])
+    else:
+        m = jf.box_mesh_tet10(nx, ny, nz, Lx, Ly, Lz)
+        pts, cells = np.array(m.points), np.asarray(m.cells_dict["tetra10"])
+        if ele == "TET4":
+            nv = (nx + 1) * (ny + 1) * (nz + 1)
+            pts, cells = pts[:nv], cells[:, :4]
+    t = basis.element_tables(ele)
+    box = Lx * Ly * Lz
+    inner = np.all((pts > 1e-9) & (pts < np.array([Lx, Ly, Lz]) - 1e-9), axis=1)
+    moved = pts.copy()
+    moved[inner] += np.random.default_rng(3).uniform(-0.2, 0.2, (inner.sum(), 3)) * (Lx / nx)
+    V = omma.cell_volume(pts if ele == "TET10" else moved, cells, t["shape_grads_ref"], t["quad_weights"])
+    assert abs(V - box) <= 1e-14 * box, (ele, V)
+    if ele == "TET10":
+        Vm = omma.cell_volume(moved, cells, t["shape_grads_ref"], t["quad_weights"])
+        Vo = ofem.OracleFE(moved, cells, 3, ele).JxW.sum()
+        assert abs(Vm - Vo) <= 1e-14 * box
 
 
 def test_oracle_filter_uniform_grid_weights():
