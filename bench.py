@@ -164,7 +164,8 @@ def spmv_roofline(prob, peak):
     input vector prepared once).  DF48 is timed through fem_spmv_dfx, the kernel the mixed CG
     runs (node-interleaved double-float x, double-float y, fused dot).  Algorithmic bytes per
     launch: values (6 B/nnz DF48, 8 B FP64, 4 B FP32) + one 4-byte block column per vec*vec
-    values + slice or row pointers + x read + y write."""
+    values + slice or row pointers + x read + y write (no block columns for the DF48 copy in the
+    grid layout of a box-numbered mesh)."""
     import ctypes as C
     import torch
     import jax_fem_gb300 as jf
@@ -223,6 +224,9 @@ def spmv_roofline(prob, peak):
             # transposed part (atomics), both written once per dof
             nb_u = (nnzb - eng.num_nodes) // 2 + eng.num_nodes
             algo = nb_u * eng.vec ** 2 * es + nb_u * 4 + (eng.n_slices + 1) * 8 + n * xs + n * ys
+        elif prec == L_.FEM_SLICED_DF48 and eng.slices_grid:
+            # grid layout (box numbering): the block columns follow from the node grid, none is read
+            algo = nnz * es + (eng.n_slices + 1) * 8 + n * xs + n * ys
         else:
             algo = nnz * es + nnzb * 4 + (eng.num_nodes + 1) * 8 + n * xs + n * ys
         out[name] = {"seconds": t, "algorithmic_bytes": algo, "achieved_gbs": algo / t / 1e9,
@@ -297,7 +301,7 @@ def measured_peak():
 
 
 TRAFFIC_PROFILES = {
-    "df48": os.path.join(ROOT, "profiles", "spmv_sliced_dfdf_bulk_hex8_160x80x40.txt"),
+    "df48": os.path.join(ROOT, "profiles", "spmv_sliced_dfdf_bulk_grid_hex8_160x80x40.txt"),
     "sym_df48": os.path.join(ROOT, "profiles", "spmv_sym_df48_bulk_hex8_100x50x25.txt"),
 }
 

@@ -129,6 +129,8 @@ typedef struct fem_pattern_t {
   const int32_t* slice_cols_u;/* padding: the row's own node                         */
   int64_t grid_nx, grid_ny, grid_nz; /* node grid of a structured box numbering          */
                             /* node = (i*ny + j)*nz + k, or 0 when not structured   */
+  int64_t slices_grid;      /* 1: slice_ptr / slice_cols are the grid layout of      */
+                            /* fem_pattern_slices_grid (slot k = stencil offset k)  */
 } fem_pattern_t;
 
 typedef struct fem_material_t {
@@ -306,6 +308,17 @@ int fem_spmv(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int32_t pre
  * n_slices = ceil(n_nodes/32)) and the slot count (host; syncs); otherwise fills slice_cols. */
 int fem_pattern_slices(int64_t n_nodes, const int64_t* block_ptr, const int32_t* block_cols,
                        int64_t* slice_ptr, int32_t* slice_cols, int64_t* n_slots, void* stream);
+/* Sliced layout of a pattern on the node grid nx x ny x nz (node = (i*ny + j)*nz + k, the
+ * numbering of box_mesh) whose node rows hold only 27-point-stencil neighbours (HEX8, TET4): every
+ * slice has 27 slots, slot k = (di+1)*9 + (dj+1)*3 + (dk+1) holding the block of neighbour
+ * (i+di, j+dj, k+dk), a zero block where that neighbour is outside the grid or not coupled.
+ * slice_ptr (n_slices+1) = 27 s; slice_cols (27*n_slices*32) = node + offset of slot k, clamped
+ * to [0, n_nodes).  n_slots = 27*n_slices.  The column of every slot follows from the grid, so the
+ * mixed CG's SpMV streams no block columns.  Fails with FEM_ERR_ARG (slice_ptr then undefined)
+ * when a row holds a block outside the stencil.  Set fem_pattern_t.slices_grid = 1 with these
+ * arrays.  Syncs. */
+int fem_pattern_slices_grid(int64_t n_nodes, const int64_t* block_ptr, const int32_t* block_cols, int64_t nx,
+                            int64_t ny, int64_t nz, int64_t* slice_ptr, int32_t* slice_cols, void* stream);
 /* The same for the upper node blocks of each row (block column >= row): slice_ptr_u,
  * slice_cols_u and n_slots_u of the FEM_SYM_DF48 layout. */
 int fem_pattern_slices_upper(int64_t n_nodes, const int64_t* block_ptr, const int32_t* block_cols,

@@ -43,7 +43,7 @@ class FemPattern(C.Structure):
                 ("n_slices", C.c_int64), ("n_slots", C.c_int64), ("slice_ptr", C.c_void_p),
                 ("slice_cols", C.c_void_p), ("n_slots_u", C.c_int64), ("slice_ptr_u", C.c_void_p),
                 ("slice_cols_u", C.c_void_p), ("grid_nx", C.c_int64), ("grid_ny", C.c_int64),
-                ("grid_nz", C.c_int64)]
+                ("grid_nz", C.c_int64), ("slices_grid", C.c_int64)]
 
 
 class FemJitParams(C.Structure):
@@ -100,6 +100,7 @@ SIGNATURES = {
     "fem_pcg_refined": ([PPAT, I64, I32, I32, P, I32, P, PMESH, PMAT, P, P, I32, P, P, P, F64, F64, F64, I64, P, SZ,
                          PI64, PI64, PF64, PI32, P], C.c_int),
     "fem_pattern_slices": ([I64, P, P, P, P, PI64, P], C.c_int),
+    "fem_pattern_slices_grid": ([I64, P, P, I64, I64, I64, P, P, P], C.c_int),
     "fem_matrix_bytes": ([PPAT, I32, I32, PSZ], C.c_int),
     "fem_matrix_convert": ([PPAT, I64, I32, P, I32, P, P], C.c_int),
     "fem_vector_split": ([P, I64, P, P], C.c_int),

@@ -113,4 +113,17 @@ __device__ __forceinline__ void sum_partials(const double* partials, int n, doub
   block_sum<NV>(out, sh);
 }
 
+// Grid stencil: slot k = (di+1)*9 + (dj+1)*3 + (dk+1) of node n = (i*ny + j)*nz + k.  Its column
+// offset (the same for every node) and the neighbour's node id, or -1 outside the grid.  Node
+// ids grow with (i, j, k) in lexicographic order, so the in-grid slots of a row come in the order
+// of its sorted block columns.
+__host__ __device__ __forceinline__ int64_t stencil_offset(int k, int64_t ny, int64_t nz) {
+  return ((int64_t)(k / 9 - 1) * ny + (k / 3 % 3 - 1)) * nz + (k % 3 - 1);
+}
+__device__ __forceinline__ int64_t stencil_neighbour(int64_t n, int k, int64_t nx, int64_t ny, int64_t nz) {
+  const int64_t i = n / (ny * nz) + k / 9 - 1, j = n / nz % ny + k / 3 % 3 - 1, l = n % nz + k % 3 - 1;
+  if (i < 0 || i >= nx || j < 0 || j >= ny || l < 0 || l >= nz) return -1;
+  return (i * ny + j) * nz + l;
+}
+
 }  // namespace fem

@@ -666,13 +666,18 @@ struct BulkGeom {
 // row); row i accumulates A_ij x_j in double-float as before and, for j != i, adds A_ij^T x_i to
 // row j through FP64 atomics into qT (zeroed by the caller, combined by the consumer).  The
 // fused dot is x.(A x) = sum_i 2 x_i.(sum_j A_ij x_j) - x_i.A_ii x_i.
-template <int VEC, bool SYM = false>
+// GRID: the grid layout of fem_pattern_slices_grid (node grid gnx x gny x gnz) -- slot k of every
+// slice couples node n with node n + stencil_offset(k) (clamped to the node range; the slots
+// outside the grid hold zero blocks), so no block columns are streamed.  Lane k < 27 holds offset
+// k; a slot reads it by one warp shuffle.
+template <int VEC, bool SYM = false, bool GRID = false>
 __global__ void __launch_bounds__(BULK_WARPS * 32)
 spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* __restrict__ sp,
                              const int32_t* __restrict__ scols, const float* __restrict__ vals,
                              const int16_t* __restrict__ vlo, const float2* __restrict__ xp,
                              float* __restrict__ yh, float* __restrict__ yl, KCtl* C, int op, double* partials,
-                             double* __restrict__ qT = nullptr) {
+                             double* __restrict__ qT = nullptr, int64_t gny = 0, int64_t gnz = 0) {
+  static_assert(!(GRID && SYM), "the grid layout holds whole rows");
   using G = BulkGeom<VEC>;
   constexpr int VV = VEC * VEC;
   constexpr int PAD = DfNode<VEC>::PAD;
@@ -683,6 +688,7 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
   unsigned char* ring = smem + G::BAR_BYTES + (size_t)wib * BULK_STAGES * G::STAGE;
   const int64_t warp = (int64_t)blockIdx.x * BULK_WARPS + wib;
   const int64_t nwarps = (int64_t)gridDim.x * BULK_WARPS;
+  const int32_t lane_off = GRID && lane < 27 ? (int32_t)stencil_offset(lane, gny, gnz) : 0;
   if (lane == 0) {
 #pragma unroll
     for (int j = 0; j < BULK_STAGES; ++j) mbar_init(bars + j, 1);
@@ -704,11 +710,11 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
       unsigned char* st = ring + (size_t)stage * G::STAGE;
       const uint32_t nb = (uint32_t)cnt;
       async_proxy_fence();
-      mbar_expect_tx(bars + stage, nb * (G::VB + G::LB + G::CB));
+      mbar_expect_tx(bars + stage, nb * (G::VB + G::LB + (GRID ? 0u : G::CB)));
       const uint64_t pol = l2_evict_first_policy();
       bulk_load_hint(st, vals + pk * VV * 32, nb * G::VB, bars + stage, pol);
       bulk_load_hint(st + BULK_SLOTS * G::VB, vlo + pk * VV * 32, nb * G::LB, bars + stage, pol);
-      bulk_load_hint(st + BULK_SLOTS * (G::VB + G::LB), scols + pk * 32, nb * G::CB, bars + stage, pol);
+      if (!GRID) bulk_load_hint(st + BULK_SLOTS * (G::VB + G::LB), scols + pk * 32, nb * G::CB, bars + stage, pol);
     }
     pk += cnt;
     return true;
@@ -722,8 +728,8 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
   float ds = 0.f, de = 0.f;
   float dd_h = 0.f, dd_l = 0.f;   // SYM: sum of x_i.A_ii x_i
   int stage = 0;
-  int64_t cs = warp, ck = 0, ce = 0;
-  if (cs < n_slices) { ck = sp[cs]; ce = sp[cs + 1]; }
+  int64_t cs = warp, ck = 0, ce = 0, cb = 0;   // cb: the slice's first slot (GRID)
+  if (cs < n_slices) { ck = cb = sp[cs]; ce = sp[cs + 1]; }
   float sh[VEC], sl[VEC];
 #pragma unroll
   for (int r = 0; r < VEC; ++r) { sh[r] = 0.f; sl[r] = 0.f; }
@@ -761,8 +767,18 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
       const int cnt = ce - ck < BULK_SLOTS ? (int)(ce - ck) : BULK_SLOTS;
       float xvh[BULK_SLOTS][VEC], xvl[BULK_SLOTS][VEC];
 #pragma unroll
-      for (int t = 0; t < BULK_SLOTS; ++t)
-        if (t < cnt) df_gather<VEC>(xp, sc[t * 32 + lane], xvh[t], xvl[t]);
+      for (int t = 0; t < BULK_SLOTS; ++t) {
+        if (t < cnt) {
+          int64_t col;
+          if constexpr (GRID) {
+            col = cs * 32 + lane + __shfl_sync(0xffffffffu, lane_off, (int)(ck - cb) + t);
+            col = col < 0 ? 0 : col >= n_nodes ? n_nodes - 1 : col;
+          } else {
+            col = sc[t * 32 + lane];
+          }
+          df_gather<VEC>(xp, col, xvh[t], xvl[t]);
+        }
+      }
       if constexpr (PAIR) {
         // the stage's two slots as the two components of paired FP32 operations; a stage with one
         // slot (a slice's odd last one) pairs it with zeros -- a warp-uniform branch, so the full
@@ -869,7 +885,7 @@ spmv_sliced_dfdf_bulk_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* _
 #pragma unroll
       for (int r = 0; r < VEC; ++r) { sh[r] = 0.f; sl[r] = 0.f; }
       cs += nwarps;
-      if (cs < n_slices) { ck = sp[cs]; ce = sp[cs + 1]; }
+      if (cs < n_slices) { ck = cb = sp[cs]; ce = sp[cs + 1]; }
       load_own();
     }
   }
@@ -909,10 +925,13 @@ __global__ void sym_combine_kernel(int64_t n_nodes, float* __restrict__ yh, floa
 #include "fem_ssym.cuh"
 namespace fem {
 
-// FP64 CSR values -> sliced layout (FP64, FP32 or DF48 hi/lo), thread per (slice, lane).
+// FP64 CSR values -> sliced layout (FP64, FP32 or DF48 hi/lo), thread per (slice, lane).  Slot k
+// of a row holds its k-th block, or with the grid layout (gnx > 0, fem_pattern_slices_grid) the
+// block of stencil neighbour k, found by a merge walk over the row's sorted block columns.
 template <int VEC, int OUT>
 __global__ void to_sliced_kernel(int64_t n_nodes, int64_t n_slices, const int64_t* bp, const int64_t* sp,
-                                 const double* v64, void* out, int16_t* lo) {
+                                 const double* v64, void* out, int16_t* lo, const int32_t* bcols, int64_t gnx,
+                                 int64_t gny, int64_t gnz) {
   constexpr int VV = VEC * VEC;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_slices * 32; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t s = t >> 5;
@@ -921,10 +940,20 @@ __global__ void to_sliced_kernel(int64_t n_nodes, int64_t n_slices, const int64_
     const int64_t b0 = i < n_nodes ? bp[i] : 0;
     const int nb = i < n_nodes ? (int)(bp[i + 1] - b0) : 0;
     const int64_t w = sp[s + 1] - sp[s];
+    int p = 0;   // grid layout: merge cursor into the row's block columns
     for (int64_t k = 0; k < w; ++k) {
+      int blk = k < nb ? (int)k : -1;
+      if (gnx > 0) {
+        blk = -1;
+        const int64_t j = i < n_nodes ? stencil_neighbour(i, (int)k, gnx, gny, gnz) : -1;
+        if (j >= 0) {
+          while (p < nb && bcols[b0 + p] < j) ++p;
+          if (p < nb && bcols[b0 + p] == j) blk = p;
+        }
+      }
       for (int v = 0; v < VV; ++v) {
         const int r = v / VEC, d = v % VEC;
-        const double a = k < nb ? v64[(int64_t)VV * b0 + (int64_t)r * VEC * nb + VEC * k + d] : 0.0;
+        const double a = blk >= 0 ? v64[(int64_t)VV * b0 + (int64_t)r * VEC * nb + VEC * blk + d] : 0.0;
         const int64_t o = ((sp[s] + k) * VV + v) * 32 + l;
         if (OUT == FEM_SLICED_F64) {
           static_cast<double*>(out)[o] = a;
@@ -2157,22 +2186,36 @@ static int launch_dfdf(const fem_pattern_t* pat, int64_t n_nodes, const float* v
   const bool bulk = VEC == 3 && aligned16(vhi) && aligned16(vlo) && aligned16(sc);
   if (SYM && !(bulk && qT)) return fail(FEM_ERR_ARG, "FEM_SYM_DF48 needs vec 3 and 16-byte aligned arrays");
   if (bulk) {
-    auto kern = spmv_sliced_dfdf_bulk_kernel<VEC, SYM>;
     constexpr int smem = (int)BulkGeom<VEC>::SMEM;
-    static int per_sm = 0;
-    if (per_sm == 0) {
-      cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-      if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BULK_WARPS * 32, smem) != cudaSuccess ||
-          per_sm < 1)
-        per_sm = 1;
+    auto prepare = [&](auto kern, int& per_sm) -> unsigned {
+      if (per_sm == 0) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BULK_WARPS * 32, smem) != cudaSuccess ||
+            per_sm < 1)
+          per_sm = 1;
+      }
+      int64_t g = (int64_t)sm_count() * per_sm;
+      const int64_t need = (ns + BULK_WARPS - 1) / BULK_WARPS;
+      if (g > need) g = need;
+      if (g > MAX_PARTIAL_BLOCKS) g = MAX_PARTIAL_BLOCKS;
+      return (unsigned)(g < 1 ? 1 : g);
+    };
+    if constexpr (!SYM && VEC == 3) {
+      if (pat->slices_grid) {   // grid layout: columns from the stencil, none streamed
+        auto kern = spmv_sliced_dfdf_bulk_kernel<VEC, false, true>;
+        static int per_sm_grid = 0;
+        const unsigned g = prepare(kern, per_sm_grid);
+        kern<<<g, BULK_WARPS * 32, smem, s>>>(n_nodes, ns, sp, sc, vhi, vlo, xp, yh, yl, C, op, partials, qT,
+                                              pat->grid_ny, pat->grid_nz);
+        note_launches(1);
+        return FEM_OK;
+      }
     }
-    int64_t g = (int64_t)sm_count() * per_sm;
-    const int64_t need = (ns + BULK_WARPS - 1) / BULK_WARPS;
-    if (g > need) g = need;
-    if (g > MAX_PARTIAL_BLOCKS) g = MAX_PARTIAL_BLOCKS;
-    if (g < 1) g = 1;
-    kern<<<(unsigned)g, BULK_WARPS * 32, smem, s>>>(n_nodes, ns, sp, sc, vhi, vlo, xp, yh, yl, C, op, partials, qT);
+    auto kern = spmv_sliced_dfdf_bulk_kernel<VEC, SYM>;
+    static int per_sm = 0;
+    const unsigned g = prepare(kern, per_sm);
+    kern<<<g, BULK_WARPS * 32, smem, s>>>(n_nodes, ns, sp, sc, vhi, vlo, xp, yh, yl, C, op, partials, qT, 0, 0);
   } else {
     auto kern = spmv_sliced_dfdf_kernel<VEC>;
     static int per_sm = 0;
@@ -2773,6 +2816,10 @@ static int check_pat(const fem_pattern_t* pat, int64_t n_nodes, int32_t vec, int
               "FEM_SSYM_DF48 needs vec 3 and the pattern's node grid (grid_nx*grid_ny*grid_nz == n_nodes)");
   FEM_REQUIRE(!is_sliced(precision) || (pat->n_slices == (n_nodes + 31) / 32 && pat->slice_ptr && pat->slice_cols),
               "sliced format needs the pattern's slice arrays (fem_pattern_slices)");
+  FEM_REQUIRE(!pat->slices_grid || (pat->grid_nx > 0 && pat->grid_ny > 0 && pat->grid_nz > 0 &&
+                                    pat->grid_nx * pat->grid_ny * pat->grid_nz == n_nodes &&
+                                    pat->n_slots == 27 * pat->n_slices),
+              "slices_grid needs the node grid and the 27-slot layout of fem_pattern_slices_grid");
   FEM_REQUIRE(precision != FEM_SYM_DF48 || (pat->slice_ptr_u && pat->slice_cols_u && pat->n_slots_u > 0),
               "FEM_SYM_DF48 needs the upper-block slice arrays (fem_pattern_slices_upper)");
   return FEM_OK;
@@ -3119,9 +3166,11 @@ extern "C" int fem_matrix_convert(const fem_pattern_t* pat, int64_t n_nodes, int
     const int64_t m = n_values(pat, vec, precision);
     int16_t* lo = is_df(precision) ? reinterpret_cast<int16_t*>((char*)out + df_lo_offset(m)) : nullptr;
     const int g = grid_for(pat->n_slices * 32, 256);
+    const bool gl = pat->slices_grid != 0;
 #define FEM_TO_SLICED(VEC, OUT)                                                                              \
   to_sliced_kernel<VEC, OUT><<<g, 256, 0, s>>>(n_nodes, pat->n_slices, pat->block_ptr, pat->slice_ptr, vals64, \
-                                                out, lo)
+                                                out, lo, pat->block_cols, gl ? pat->grid_nx : 0, pat->grid_ny, \
+                                                pat->grid_nz)
     if (vec == 3) {
       if (precision == FEM_SLICED_F64) FEM_TO_SLICED(3, FEM_SLICED_F64);
       else if (precision == FEM_SLICED_F32) FEM_TO_SLICED(3, FEM_SLICED_F32);

@@ -343,6 +343,41 @@ __global__ void slice_cols_kernel(int64_t n_nodes, int64_t n_slices, const int64
       scols[(sp[s] + k) * 32 + l] = k < nb ? bcols[b0 + k] : 0;
   }
 }
+// Grid layout: every block of row n must couple a stencil neighbour (|di|, |dj|, |dk| <= 1);
+// a row that does not sets *bad (thread per node row).
+__global__ void slice_grid_check_kernel(int64_t n_nodes, const int64_t* bp, const int32_t* bcols, int64_t ny,
+                                        int64_t nz, unsigned long long* bad) {
+  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = n / (ny * nz), j = n / nz % ny, k = n % nz;
+    bool ok = true;
+    for (int64_t b = bp[n]; b < bp[n + 1]; ++b) {
+      const int64_t c = bcols[b];
+      if (c < 0 || c >= n_nodes) { ok = false; break; }
+      const int64_t di = c / (ny * nz) - i, dj = c / nz % ny - j, dk = c % nz - k;
+      if (di < -1 || di > 1 || dj < -1 || dj > 1 || dk < -1 || dk > 1) { ok = false; break; }
+    }
+    if (!ok) atomicOr(bad, 1ull);
+  }
+}
+
+// Grid layout: slice_ptr[s] = 27 s; slice_cols of slot k, lane l = node + stencil offset k,
+// clamped to the node range (thread per (slice, lane)).
+__global__ void slice_grid_cols_kernel(int64_t n_nodes, int64_t n_slices, int64_t ny, int64_t nz, int64_t* sp,
+                                       int32_t* scols) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_slices * 32; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = t >> 5;
+    const int l = (int)(t & 31);
+    const int64_t n = s * 32 + l;
+    for (int k = 0; k < 27; ++k) {
+      int64_t c = n + stencil_offset(k, ny, nz);
+      c = c < 0 ? 0 : c >= n_nodes ? n_nodes - 1 : c;
+      scols[(s * 27 + k) * 32 + l] = (int32_t)c;
+    }
+    if (l == 0) sp[s] = s * 27;
+    if (t == 0) sp[n_slices] = n_slices * 27;
+  }
+}
+
 // Upper node blocks of row i: the suffix of its sorted block columns starting at the first
 // column >= i (the diagonal).
 __device__ __forceinline__ int64_t first_upper(const int32_t* bcols, int64_t b0, int64_t nb, int64_t i) {
@@ -405,6 +440,30 @@ extern "C" int fem_pattern_slices_upper(int64_t n_nodes, const int64_t* block_pt
                                                                         slice_ptr_u, slice_cols_u);
   note_launches(1);
   return check_launch("upper slice cols");
+}
+
+extern "C" int fem_pattern_slices_grid(int64_t n_nodes, const int64_t* block_ptr, const int32_t* block_cols,
+                                       int64_t nx, int64_t ny, int64_t nz, int64_t* slice_ptr, int32_t* slice_cols,
+                                       void* stream) {
+  FEM_REQUIRE(n_nodes > 0 && block_ptr && block_cols && slice_ptr && slice_cols, "bad arguments");
+  FEM_REQUIRE(nx > 0 && ny > 0 && nz > 0 && nx * ny * nz == n_nodes, "the node grid must hold n_nodes nodes");
+  FEM_REQUIRE(n_nodes < (int64_t(1) << 31), "node ids must fit int32");
+  cudaStream_t s = as_stream(stream);
+  const int64_t n_slices = (n_nodes + 31) / 32;
+  unsigned long long* bad = reinterpret_cast<unsigned long long*>(slice_ptr + n_slices);
+  FEM_CUDA(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), s));
+  slice_grid_check_kernel<<<grid_for(n_nodes, 256), 256, 0, s>>>(n_nodes, block_ptr, block_cols, ny, nz, bad);
+  note_launches(1);
+  int rc = check_launch("grid slice check");
+  if (rc) return rc;
+  unsigned long long h = 0;
+  FEM_CUDA(cudaMemcpyAsync(&h, bad, sizeof(h), cudaMemcpyDeviceToHost, s));
+  FEM_CUDA(cudaStreamSynchronize(s));
+  if (h) return fail(FEM_ERR_ARG, "fem_pattern_slices_grid: a node row couples a node outside its 27-point stencil");
+  slice_grid_cols_kernel<<<grid_for(n_slices * 32, 256), 256, 0, s>>>(n_nodes, n_slices, ny, nz, slice_ptr,
+                                                                       slice_cols);
+  note_launches(1);
+  return check_launch("grid slice cols");
 }
 
 extern "C" int fem_pattern_slices(int64_t n_nodes, const int64_t* block_ptr, const int32_t* block_cols,

@@ -280,34 +280,47 @@ class Engine:
         call("fem_pattern_scalar", self.num_nodes, self.vec, ptr(self.block_ptr), ptr(self.block_cols),
              ptr(self.indptr), ptr(self.diag), None, s)
         self.nnz = self.nnzb * self.vec * self.vec
-        # sliced layout (32 node rows per slice) of the solver copies of the matrix
+        # node grid of a structured box numbering (the grid layout below and the FEM_SSYM_DF48
+        # solver copy), vec 3 and elements whose nodes couple only grid neighbours
+        self.grid = structured_grid(self.fe.points) if self.vec == 3 and self.fe.ele_type in ("HEX8", "TET4") \
+            else None
+        # sliced layout (32 node rows per slice) of the solver copies of the matrix: on the node grid
+        # 27 stencil slots per slice whose columns follow from the grid, else each row's blocks in order
         self.n_slices = (self.num_nodes + 31) // 32
         self.slice_ptr = torch.empty(self.n_slices + 1, dtype=torch.int64, device=dev)
-        n_slots = C.c_int64()
-        call("fem_pattern_slices", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols), ptr(self.slice_ptr),
-             None, C.byref(n_slots), s)
-        self.n_slots = n_slots.value
-        self.slice_cols = torch.empty(self.n_slots * 32, dtype=torch.int32, device=dev)
-        call("fem_pattern_slices", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols), ptr(self.slice_ptr),
-             ptr(self.slice_cols), None, s)
+        self.slices_grid = False
+        if self.grid is not None:
+            self.n_slots = 27 * self.n_slices
+            self.slice_cols = torch.empty(self.n_slots * 32, dtype=torch.int32, device=dev)
+            try:
+                call("fem_pattern_slices_grid", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols),
+                     *self.grid, ptr(self.slice_ptr), ptr(self.slice_cols), s)
+                self.slices_grid = True
+            except _lib.FemError as exc:
+                logger.info("grid slice layout refused (%s); general sliced layout", exc)
+        if not self.slices_grid:
+            n_slots = C.c_int64()
+            call("fem_pattern_slices", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols), ptr(self.slice_ptr),
+                 None, C.byref(n_slots), s)
+            self.n_slots = n_slots.value
+            self.slice_cols = torch.empty(self.n_slots * 32, dtype=torch.int32, device=dev)
+            call("fem_pattern_slices", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols), ptr(self.slice_ptr),
+                 ptr(self.slice_cols), None, s)
         # upper node blocks only: the symmetric DF48 solver copy (FEM_SYM_DF48)
         self.slice_ptr_u = torch.empty(self.n_slices + 1, dtype=torch.int64, device=dev)
+        n_slots_u = C.c_int64()
         call("fem_pattern_slices_upper", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols),
-             ptr(self.slice_ptr_u), None, C.byref(n_slots), s)
-        self.n_slots_u = n_slots.value
+             ptr(self.slice_ptr_u), None, C.byref(n_slots_u), s)
+        self.n_slots_u = n_slots_u.value
         self.slice_cols_u = torch.empty(self.n_slots_u * 32, dtype=torch.int32, device=dev)
         call("fem_pattern_slices_upper", self.num_nodes, ptr(self.block_ptr), ptr(self.block_cols),
              ptr(self.slice_ptr_u), ptr(self.slice_cols_u), None, s)
-        # node grid of a structured box numbering (the FEM_SSYM_DF48 solver copy), vec 3 and
-        # elements whose nodes couple only grid neighbours
-        self.grid = structured_grid(self.fe.points) if self.vec == 3 and self.fe.ele_type in ("HEX8", "TET4") \
-            else None
         gx, gy, gz = self.grid if self.grid is not None else (0, 0, 0)
         self.pattern = _lib.FemPattern(self.nnzb, self.block_ptr.data_ptr(), self.block_cols.data_ptr(),
                                        self.indptr.data_ptr(), self.diag.data_ptr(), self.slots.data_ptr(),
                                        self.n_slices, self.n_slots, self.slice_ptr.data_ptr(),
                                        self.slice_cols.data_ptr(), self.n_slots_u, self.slice_ptr_u.data_ptr(),
-                                       self.slice_cols_u.data_ptr(), gx, gy, gz)
+                                       self.slice_cols_u.data_ptr(), gx, gy, gz, int(self.slices_grid))
         self._indices = None
 
     def scalar_indices(self):
@@ -485,7 +498,8 @@ class Engine:
                 # no structured copy for this mesh, the general sliced layout instead
                 logger.info("structured symmetric storage refused (%s); sliced DF48 instead", exc)
                 self.grid = None
-                self.pattern.grid_nx = self.pattern.grid_ny = self.pattern.grid_nz = 0
+                if not self.slices_grid:     # the grid sliced layout still reads the node grid
+                    self.pattern.grid_nx = self.pattern.grid_ny = self.pattern.grid_nz = 0
                 return self.tangent(dofs, _lib.FEM_SLICED_DF48, bc_mode, cache=cache)
             view = buf.view(torch.float64) if precision == _lib.FEM_SLICED_F64 else \
                 buf.view(torch.float32) if precision == _lib.FEM_SLICED_F32 else buf

@@ -126,6 +126,24 @@ def test_geometry_cache_and_df_assembly_validate_arguments(lib):
         assert rc == L.FEM_ERR_ARG and "precision" in L.last_error()
 
 
+def test_grid_slices_validate_arguments(lib):
+    """fem_pattern_slices_grid rejects NULL arrays and a node grid that does not hold n_nodes
+    nodes, and the solvers reject a pattern flagged with the grid layout whose slot count or grid
+    does not match it, all before touching the device."""
+    import ctypes as C
+    import jax_fem_gb300 as jf
+    L = jf._lib
+    buf = (C.c_int64 * 64)()
+    a = C.addressof(buf)
+    assert lib.fem_pattern_slices_grid(8, a, a, 2, 2, 2, a, None, None) == L.FEM_ERR_ARG
+    assert lib.fem_pattern_slices_grid(8, a, a, 2, 2, 3, a, a, None) == L.FEM_ERR_ARG
+    assert "grid" in L.last_error()
+    pat = L.FemPattern(1, a, a, a, a, a, 1, 26, a, a, 0, None, None, 2, 2, 2, 1)
+    y = (C.c_double * 24)()
+    assert lib.fem_spmv(C.byref(pat), 8, 3, L.FEM_SLICED_F64, a, y, y, None) == L.FEM_ERR_ARG
+    assert "slices_grid" in L.last_error()
+
+
 def test_element_tables_match_oracle(lib):
     from jax_fem_gb300 import basis
     from oracle import basis as ob

@@ -1,5 +1,7 @@
 """GPU parity tests: the CUDA path (through the C ABI) against the CPU oracle and the
 reference's FEniCSx gold fixtures.  Tolerances are stated per test."""
+import importlib
+
 import numpy as np
 import pytest
 import torch
@@ -578,6 +580,104 @@ def test_spmv_dfx_matches_fp64(cuda, n, kind):
         assert (y - y64).abs().max().item() <= 1e-11 * y64.abs().max().item()
         ref = torch.dot(x, y64).item()
         assert abs(dot.item() - ref) <= 1e-11 * abs(ref)
+
+
+@pytest.mark.parametrize("n", [(1, 1, 1), (3, 40, 2), (2, 2, 60), (10, 5, 3), (64, 40, 40)])
+def test_grid_slices_match_general_layout(cuda, n):
+    """On a box mesh the sliced solver copies use the grid layout (fem_pattern_slices_grid: 27
+    stencil slots per slice, the columns implied by the grid; (1,1,1) is a 2x2x2 node grid, where
+    two slots of a row share a column offset and only the in-grid one may hold the block).  The
+    same FP64 matrix converted into the general layout (fem_pattern_slices) gives the same FP64
+    sliced SpMV (equal: the grid layout only adds zero blocks to the same accumulation order) and
+    the mixed CG's SpMV within 1e-13 of |A| |x| per row and the dot within 1e-13 of |x|.|A| |x|
+    (double-float rounding, ~2^-46 of each row's sum of |a x|, differs because the layouts pair
+    different slots on the paired FP32 instructions)."""
+    import ctypes as C
+    import jax_fem_gb300 as jf
+    import cases
+    L = jf._lib
+    prob, _, theta_np = cases.simp_box(*n)
+    prob.set_params(torch.tensor(theta_np, device=cuda))
+    eng = prob._engine
+    assert eng.slices_grid and eng.pattern.slices_grid == 1 and eng.n_slots == 27 * eng.n_slices
+    z = torch.zeros(eng.num_dofs, dtype=torch.float64, device=cuda)
+    A64 = eng.tangent(z, L.FEM_F64, L.FEM_BC_SYMMETRIC, cache=False)
+    st = L.stream_handle()
+    gen = L.FemPattern.from_buffer_copy(eng.pattern)
+    sp = torch.empty(eng.n_slices + 1, dtype=torch.int64, device=cuda)
+    n_slots = C.c_int64()
+    L.call("fem_pattern_slices", eng.num_nodes, L.ptr(eng.block_ptr), L.ptr(eng.block_cols), L.ptr(sp), None,
+           C.byref(n_slots), st)
+    sc = torch.empty(n_slots.value * 32, dtype=torch.int32, device=cuda)
+    L.call("fem_pattern_slices", eng.num_nodes, L.ptr(eng.block_ptr), L.ptr(eng.block_cols), L.ptr(sp), L.ptr(sc),
+           None, st)
+    gen.slice_ptr, gen.slice_cols, gen.n_slots, gen.slices_grid = sp.data_ptr(), sc.data_ptr(), n_slots.value, 0
+
+    def convert(pat, fmt):
+        nb = C.c_size_t()
+        L.call("fem_matrix_bytes", C.byref(pat), 3, fmt, C.byref(nb))
+        buf = torch.empty(nb.value, dtype=torch.uint8, device=cuda)
+        L.call("fem_matrix_convert", C.byref(pat), eng.num_nodes, 3, L.ptr(A64.data), fmt, L.ptr(buf), st)
+        return buf
+
+    g = torch.Generator(device=cuda).manual_seed(5)
+    x = torch.randn(eng.num_dofs, dtype=torch.float64, device=cuda, generator=g)
+
+    def spmv64(pat):
+        vals = convert(pat, L.FEM_SLICED_F64)
+        y = torch.empty(eng.num_dofs, dtype=torch.float64, device=cuda)
+        L.call("fem_spmv", C.byref(pat), eng.num_nodes, 3, L.FEM_SLICED_F64, L.ptr(vals), L.ptr(x), L.ptr(y), st)
+        return y
+
+    y_grid, y_gen = spmv64(eng.pattern), spmv64(gen)
+    assert torch.equal(y_grid, y_gen)
+    assert (y_grid - A64.matvec(x)).abs().max().item() <= 1e-13 * y_gen.abs().max().item()
+
+    nb = C.c_size_t()
+    L.call("fem_krylov_workspace", eng.num_dofs, L.FEM_SLICED_DF48, C.byref(nb))
+    ws = torch.empty(nb.value, dtype=torch.uint8, device=cuda)
+    xp = _df_nodes(x, 3)
+
+    def spmv_df(pat):
+        vals = convert(pat, L.FEM_SLICED_DF48)
+        yh = torch.empty(eng.num_dofs, dtype=torch.float32, device=cuda)
+        yl = torch.empty_like(yh)
+        dot = torch.zeros(1, dtype=torch.float64, device=cuda)
+        L.call("fem_spmv_dfx", C.byref(pat), eng.num_nodes, 3, L.FEM_SLICED_DF48, L.ptr(vals), L.ptr(xp), L.ptr(yh),
+               L.ptr(yl), L.ptr(dot), L.ptr(ws), nb.value, st)
+        return yh.double() + yl.double(), dot.item()
+
+    (yg, dg), (yo, do) = spmv_df(eng.pattern), spmv_df(gen)
+    DeviceCSR = importlib.import_module("jax_fem_gb300.device").DeviceCSR
+    ax = DeviceCSR(eng, L.FEM_F64, A64.data.abs(), L.FEM_BC_SYMMETRIC).matvec(x.abs())
+    assert torch.all((yg - yo).abs() <= 1e-13 * ax)
+    assert abs(dg - do) <= 1e-13 * torch.dot(x.abs(), ax).item()
+
+
+def test_grid_slices_refuse_non_stencil_rows(cuda):
+    """fem_pattern_slices_grid refuses (FEM_ERR_ARG) a pattern with a block outside a row's 27-point
+    stencil and a grid whose size is not the node count; Problem then keeps the general layout."""
+    import jax_fem_gb300 as jf
+    import cases
+    L = jf._lib
+    prob, _, _ = cases.simp_box(4, 3, 3)
+    eng = prob._engine
+    st = L.stream_handle()
+    sp = torch.empty(eng.n_slices + 1, dtype=torch.int64, device=cuda)
+    sc = torch.empty(27 * eng.n_slices * 32, dtype=torch.int32, device=cuda)
+    cols = eng.block_cols.clone()
+    cols[-1] = 0     # the last node's last block now couples node 0, far outside its stencil
+    with pytest.raises(L.FemError) as e:
+        L.call("fem_pattern_slices_grid", eng.num_nodes, L.ptr(eng.block_ptr), L.ptr(cols), *eng.grid, L.ptr(sp),
+               L.ptr(sc), st)
+    assert e.value.code == L.FEM_ERR_ARG
+    nx, ny, nz = eng.grid
+    with pytest.raises(L.FemError):
+        L.call("fem_pattern_slices_grid", eng.num_nodes, L.ptr(eng.block_ptr), L.ptr(eng.block_cols), nx, ny, nz + 1,
+               L.ptr(sp), L.ptr(sc), st)
+    L.call("fem_pattern_slices_grid", eng.num_nodes, L.ptr(eng.block_ptr), L.ptr(eng.block_cols), nx, ny, nz,
+           L.ptr(sp), L.ptr(sc), st)
+    assert torch.equal(sp.cpu(), 27 * torch.arange(eng.n_slices + 1))
 
 
 def test_custom_solver_hook_petsc_style(cuda):
