@@ -144,6 +144,26 @@ def test_grid_slices_validate_arguments(lib):
     assert "slices_grid" in L.last_error()
 
 
+def test_structured_grid_detection():
+    """structured_grid (the host test behind the grid slice layout and FEM_SSYM_DF48) finds the
+    node grid of box_mesh's numbering (z fastest), including one-cell-thick boxes, and refuses
+    moved nodes, a permuted numbering and x-fastest numbering."""
+    import importlib
+    import jax_fem_gb300 as jf
+    D = importlib.import_module("jax_fem_gb300.device")
+    for n in ((4, 3, 2), (1, 1, 1), (5, 1, 7), (2, 6, 1)):
+        m = jf.box_mesh(*n, 2.0, 1.0, 0.5)
+        assert D.structured_grid(m.points) == tuple(k + 1 for k in n), n
+    pts = np.array(jf.box_mesh(4, 3, 2, 2.0, 1.0, 0.5).points)
+    moved = pts.copy()
+    moved[7] += 0.01
+    assert D.structured_grid(moved) is None
+    perm = np.random.default_rng(0).permutation(len(pts))
+    assert D.structured_grid(pts[perm]) is None
+    g = pts.reshape(5, 4, 3, 3).transpose(2, 1, 0, 3).reshape(-1, 3)   # x fastest
+    assert D.structured_grid(g) is None
+
+
 def test_element_tables_match_oracle(lib):
     from jax_fem_gb300 import basis
     from oracle import basis as ob
