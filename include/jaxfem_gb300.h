@@ -123,7 +123,8 @@ typedef struct fem_pattern_t {
   int64_t n_slices;         /* sliced layout (fem_pattern_slices); 0 when not built  */
   int64_t n_slots;          /* total block slots of the sliced layout (host value)    */
   const int64_t* slice_ptr; /* (n_slices+1) first block slot of each 32-node slice    */
-  const int32_t* slice_cols;/* (n_slots*32) block column of slot k, lane l (padding: 0) */
+  const int32_t* slice_cols;/* (n_slots*32) block column of slot k, lane l (padding: 0; */
+                            /* grid layout: node + stencil offset, clamped)           */
   int64_t n_slots_u;        /* upper-block sliced layout (fem_pattern_slices_upper)  */
   const int64_t* slice_ptr_u;
   const int32_t* slice_cols_u;/* padding: the row's own node                         */
