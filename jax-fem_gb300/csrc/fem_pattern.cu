@@ -446,7 +446,9 @@ extern "C" int fem_pattern_slices_grid(int64_t n_nodes, const int64_t* block_ptr
                                        int64_t nx, int64_t ny, int64_t nz, int64_t* slice_ptr, int32_t* slice_cols,
                                        void* stream) {
   FEM_REQUIRE(n_nodes > 0 && block_ptr && block_cols && slice_ptr && slice_cols, "bad arguments");
-  FEM_REQUIRE(nx > 0 && ny > 0 && nz > 0 && nx * ny * nz == n_nodes, "the node grid must hold n_nodes nodes");
+  FEM_REQUIRE(nx > 0 && ny > 0 && nz > 0 && nx <= n_nodes && ny <= n_nodes && nz <= n_nodes &&
+                  nx * ny <= n_nodes && nx * ny * nz == n_nodes,
+              "the node grid must hold n_nodes nodes");
   FEM_REQUIRE(n_nodes < (int64_t(1) << 31), "node ids must fit int32");
   cudaStream_t s = as_stream(stream);
   const int64_t n_slices = (n_nodes + 31) / 32;
